@@ -1,0 +1,154 @@
+/*
+ * sqrtsmooth: C ABI of the GB300 square-root parallel smoother.
+ *
+ * This is the drop-in boundary for the parallel-mode path of parsmooth
+ * (EEA-sensors/sqrt-parallel-smoothers).  Each entry point replaces one
+ * reference function; the citation is given beside it.  All array arguments
+ * are raw device pointers of the problem's dtype (float or double) unless
+ * stated otherwise, row-major, densely packed.  The library never allocates
+ * device memory: scratch space is a caller-provided workspace whose size comes
+ * from ss_workspace_bytes().  Every call is asynchronous on the given stream
+ * and returns an ss_status.
+ *
+ * Batches.  B independent sequences of lengths T_i are packed back to back:
+ *   observations  (sum T_i, ny), sequence i at rows [offsets[i], offsets[i+1])
+ *   trajectories  (sum (T_i + 1), nx) means and (sum (T_i + 1), nx, nx)
+ *                 lower Cholesky factors, sequence i at rows
+ *                 [offsets[i] + i, offsets[i+1] + i + 1)
+ * offsets is a device int64 array of B+1 entries with offsets[0] = 0.
+ */
+#ifndef SQRTSMOOTH_H_
+#define SQRTSMOOTH_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* ss_stream_t; /* a cudaStream_t */
+
+typedef enum {
+  SS_OK = 0,
+  SS_ERR_INVALID = 1,      /* bad argument: null pointer, size, shape (reference: TypeError/ValueError) */
+  SS_ERR_UNSUPPORTED = 2,  /* model, method or dimension not built (reference: NotImplementedError) */
+  SS_ERR_CUDA = 3,         /* a CUDA launch or runtime call failed */
+  SS_ERR_WORKSPACE = 4     /* workspace smaller than ss_workspace_bytes() */
+} ss_status;
+
+enum { SS_F32 = 0, SS_F64 = 1 };
+
+/* Linearisation methods: parsmooth/linearization/__init__.py:1-5 */
+enum {
+  SS_LIN_EXTENDED = 0,      /* parsmooth/linearization/_extended.py:9-70 */
+  SS_LIN_CUBATURE = 1,      /* parsmooth/linearization/_cubature.py:10-85 */
+  SS_LIN_UNSCENTED = 2,     /* parsmooth/linearization/_unscented.py:10-101 */
+  SS_LIN_GAUSS_HERMITE = 3  /* parsmooth/linearization/_gh.py:13-151 */
+};
+
+/* Device model registry (the reference accepts any JAX callable in
+ * FunctionalModel, parsmooth/_base.py:15-17; device code needs a known model) */
+enum {
+  SS_MODEL_LINEAR = 0,           /* f(x) = A x                       (tests/_lgssm.py:5-35) */
+  SS_MODEL_COORDINATED_TURN = 1, /* CT transition, nx = 5            (tests/bearings/bearings_utils.py:7-44) */
+  SS_MODEL_BEARINGS = 2          /* two bearings atan2, ny = 2       (tests/bearings/bearings_utils.py:47-69) */
+};
+
+/* Sigma-point regression form (see ss_lin.cuh): 0 = automatic (the
+ * reference's downdate in FP64, the cancellation-free residual form in FP32),
+ * 1 = downdate (parsmooth/linearization/_sigma_points.py:77-78), 2 = residual. */
+enum { SS_SLR_AUTO = 0 };
+
+#define SS_MAX_GH_ORDER 8
+
+/* A FunctionalModel(function, MVNSqrt(noise_mean, noise_chol)). */
+typedef struct ss_model {
+  int32_t kind;            /* SS_MODEL_* */
+  int32_t reserved;
+  const void* matrix;      /* SS_MODEL_LINEAR: (d_out, d_in) matrix A, device */
+  double params[4];        /* COORDINATED_TURN: {dt}; BEARINGS: {s1x, s1y, s2x, s2y} */
+  const void* noise_mean;  /* (d_out,), device */
+  const void* noise_chol;  /* (d_out, d_out) lower triangular, device */
+} ss_model;
+
+typedef struct ss_problem {
+  int32_t dtype;           /* SS_F32 or SS_F64 */
+  int32_t nx, ny;
+  int32_t lin_method;      /* SS_LIN_* */
+  double ut_alpha, ut_beta, ut_kappa; /* unscented parameters */
+  int32_t ut_kappa_default;/* nonzero: kappa = 3 + nx (parsmooth/linearization/_unscented.py:64-65) */
+  int32_t gh_order;        /* Gauss-Hermite order, 1..SS_MAX_GH_ORDER */
+  int32_t slr_form;        /* SS_SLR_AUTO, 1 or 2 */
+  int32_t chunk;           /* steps per level-0 chunk, 0 = default */
+  int32_t group;           /* summaries per group at higher scan levels, 0 = default */
+  int32_t reserved;
+  ss_model transition;     /* nx -> nx */
+  ss_model observation;    /* nx -> ny */
+  int64_t batch;           /* B >= 1 */
+  int64_t total_steps;     /* sum T_i */
+  int64_t max_len;         /* max T_i (upper bound is enough) */
+  const int64_t* offsets;  /* device, B + 1 */
+} ss_problem;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int ss_version(void);
+
+/* Static text of a status code. */
+const char* ss_status_string(int status);
+
+/* Nonzero if (dtype, nx, ny, lin_method, models) has compiled kernels. */
+int ss_supported(const ss_problem* p);
+
+/* Workspace bytes for any entry point below on this problem (host only). */
+int ss_workspace_bytes(const ss_problem* p, size_t* bytes);
+
+/* Linearise one model at n points x_k = N(m[k], chol[k] chol[k]^T).
+ * Replaces linearization_method(model, x) of parsmooth/linearization/*.py
+ * (e.g. _cubature.py:10-34), vectorised.  which = 0 transition, 1 observation.
+ * Outputs F (n, d_out, nx), chol (n, d_out, d_out), b (n, d_out). */
+int ss_linearize(const ss_problem* p, int32_t which, int64_t n, const void* m, const void* chol,
+                 void* F, void* chol_out, void* b, ss_stream_t stream);
+
+/* Parallel square-root filter: parsmooth/parallel/_filtering.py:13-61
+ * (methods.filtering, parsmooth/methods.py:14-26, with parallel=True).
+ * m0 (B or 1, nx), L0 (B or 1, nx, nx): prior_per_sequence selects B or 1.
+ * nominal_m / nominal_L: the linearisation trajectory or NULL for the
+ * reference's default (zero means, identity factors, _filtering.py:25-28).
+ * out_m / out_L: filtered trajectory (T+1 states per sequence).
+ * out_ell: NULL or (B,) double, the summed predictive log-likelihood
+ * (_filtering.py:53-60). */
+int ss_filter(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+              int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
+              void* out_m, void* out_L, double* out_ell, void* workspace, size_t workspace_bytes,
+              ss_stream_t stream);
+
+/* Parallel square-root RTS smoother: parsmooth/parallel/_smoothing.py:14-44
+ * (methods.smoothing, parsmooth/methods.py:29-35, parallel=True).
+ * filt_m / filt_L: a filtered trajectory; nominal: as in ss_filter. */
+int ss_smooth(const ss_problem* p, const void* filt_m, const void* filt_L, const void* nominal_m,
+              const void* nominal_L, void* out_m, void* out_L, void* workspace,
+              size_t workspace_bytes, ss_stream_t stream);
+
+/* Iterated smoother: parsmooth/methods.py:54-76 with parallel=True.
+ * init_m / init_L: initial nominal trajectory, or NULL for the reference's
+ * extra filter-smoother pass at the default nominal (:63-65).
+ * n_iter: number of filter-smoother calls (criterion "i < n_iter"), or the
+ * maximum number when tol > 0; with tol > 0 a sequence stops once the mean
+ * squared change of its means is <= tol (_default_criterion, :50-51, uses
+ * 1e-6).  out_ell: NULL or (B,) double - the log-likelihood of a final
+ * filtering pass at the converged trajectory (:72-75).  out_iters: NULL or
+ * (B,) int32 filter-smoother calls made per sequence.  out_flags: NULL or
+ * (B,) uint32 status bits: 1 non-finite output, 2 non-finite log-likelihood,
+ * 4 not converged within n_iter (tol > 0 only). */
+int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+                int32_t prior_per_sequence, const void* init_m, const void* init_L,
+                int32_t n_iter, double tol, void* out_m, void* out_L, double* out_ell,
+                int32_t* out_iters, uint32_t* out_flags, void* workspace, size_t workspace_bytes,
+                ss_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SQRTSMOOTH_H_ */

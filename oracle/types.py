@@ -1,0 +1,31 @@
+"""Oracle container types (TEST INFRASTRUCTURE ONLY).
+
+Restates ``parsmooth/_base.py:5-30``: plain named tuples, and the
+"all inputs must have the same type" check that raises ``TypeError``.
+"""
+from typing import Any, Callable, NamedTuple
+
+
+class MVNStandard(NamedTuple):
+    """Gaussian in covariance form (parsmooth/_base.py:5-7)."""
+    mean: Any
+    cov: Any
+
+
+class MVNSqrt(NamedTuple):
+    """Gaussian in square-root form, ``cov = chol @ chol.T`` (parsmooth/_base.py:10-12)."""
+    mean: Any
+    chol: Any
+
+
+class FunctionalModel(NamedTuple):
+    """``x_next = function(x) + q``, ``q ~ mvn`` (parsmooth/_base.py:15-17)."""
+    function: Callable
+    mvn: Any
+
+
+def are_inputs_compatible(*ys):
+    """Raise ``TypeError`` unless consecutive inputs share a type (parsmooth/_base.py:25-30)."""
+    types = [type(y) for y in ys]
+    if not any(a == b for a, b in zip(types[:-1], types[1:])):
+        raise TypeError(f"All inputs should have the same type. {ys} was given")

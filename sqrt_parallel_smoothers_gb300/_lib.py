@@ -1,0 +1,86 @@
+"""ctypes binding of ``libsqrtsmooth.so`` (the C ABI declared in ``include/sqrtsmooth.h``).
+
+The library is the only compute path: if it is missing or fails to load,
+every entry point raises - there is no CPU fallback.
+"""
+import ctypes
+import os
+import threading
+
+from ._build import LIB
+
+SS_OK, SS_ERR_INVALID, SS_ERR_UNSUPPORTED, SS_ERR_CUDA, SS_ERR_WORKSPACE = 0, 1, 2, 3, 4
+SS_F32, SS_F64 = 0, 1
+SS_LIN_EXTENDED, SS_LIN_CUBATURE, SS_LIN_UNSCENTED, SS_LIN_GAUSS_HERMITE = 0, 1, 2, 3
+SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS = 0, 1, 2
+SS_MAX_GH_ORDER = 8
+
+EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
+            "ss_filter", "ss_smooth", "ss_iterated")
+
+
+class SSModel(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32), ("matrix", ctypes.c_void_p),
+                ("params", ctypes.c_double * 4), ("noise_mean", ctypes.c_void_p),
+                ("noise_chol", ctypes.c_void_p)]
+
+
+class SSProblem(ctypes.Structure):
+    _fields_ = [("dtype", ctypes.c_int32), ("nx", ctypes.c_int32), ("ny", ctypes.c_int32),
+                ("lin_method", ctypes.c_int32), ("ut_alpha", ctypes.c_double), ("ut_beta", ctypes.c_double),
+                ("ut_kappa", ctypes.c_double), ("ut_kappa_default", ctypes.c_int32),
+                ("gh_order", ctypes.c_int32), ("slr_form", ctypes.c_int32), ("chunk", ctypes.c_int32),
+                ("group", ctypes.c_int32), ("reserved", ctypes.c_int32), ("transition", SSModel),
+                ("observation", SSModel), ("batch", ctypes.c_int64), ("total_steps", ctypes.c_int64),
+                ("max_len", ctypes.c_int64), ("offsets", ctypes.c_void_p)]
+
+
+_lock = threading.Lock()
+_handle = None
+
+P = ctypes.c_void_p
+PP = ctypes.POINTER(SSProblem)
+
+
+def load():
+    """Load the shared library once; raise ``RuntimeError`` if it is not built."""
+    global _handle
+    if _handle is not None:
+        return _handle
+    with _lock:
+        if _handle is not None:
+            return _handle
+        if not os.path.exists(LIB):
+            raise RuntimeError(f"sqrtsmooth CUDA library not found at {LIB}; build it with "
+                               "`python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = ctypes.CDLL(LIB)
+        lib.ss_version.restype = ctypes.c_int
+        lib.ss_status_string.restype = ctypes.c_char_p
+        lib.ss_status_string.argtypes = [ctypes.c_int]
+        lib.ss_supported.argtypes = [PP]
+        lib.ss_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
+        lib.ss_linearize.argtypes = [PP, ctypes.c_int32, ctypes.c_int64, P, P, P, P, P, P]
+        lib.ss_filter.argtypes = [PP, P, P, P, ctypes.c_int32, P, P, P, P, P, P, ctypes.c_size_t, P]
+        lib.ss_smooth.argtypes = [PP, P, P, P, P, P, P, P, ctypes.c_size_t, P]
+        lib.ss_iterated.argtypes = [PP, P, P, P, ctypes.c_int32, P, P, ctypes.c_int32, ctypes.c_double,
+                                    P, P, P, P, P, P, ctypes.c_size_t, P]
+        for name in EXPORTED:
+            getattr(lib, name).restype = ctypes.c_int if name != "ss_status_string" else ctypes.c_char_p
+        _handle = lib
+        return lib
+
+
+class SqrtSmoothError(RuntimeError):
+    """A CUDA-side failure reported by the library."""
+
+
+def check(status):
+    """Map a status code to the reference's exception types (TypeError/NotImplementedError/...)."""
+    if status == SS_OK:
+        return
+    msg = load().ss_status_string(status).decode()
+    if status == SS_ERR_INVALID:
+        raise ValueError(msg)
+    if status == SS_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    raise SqrtSmoothError(msg)

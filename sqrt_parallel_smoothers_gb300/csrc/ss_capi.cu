@@ -1,0 +1,273 @@
+// C ABI of the library: argument validation and dispatch to the compiled
+// (dtype, nx, ny) instantiations.
+#include <cmath>
+#include <cstring>
+
+#include "ss_dims.h"
+#include "ss_run.cuh"
+
+namespace ss {
+
+#define SS_DECL(NX, NY)                      \
+  int run_f32_##NX##_##NY(const Call& c);    \
+  int run_f64_##NX##_##NY(const Call& c);
+SS_FOR_DIMS(SS_DECL)
+#undef SS_DECL
+
+static RunFn find_run(int dtype, int nx, int ny) {
+#define SS_CASE(NX, NY) \
+  if (nx == NX && ny == NY) return dtype == SS_F32 ? run_f32_##NX##_##NY : run_f64_##NX##_##NY;
+  SS_FOR_DIMS(SS_CASE)
+#undef SS_CASE
+  return nullptr;
+}
+
+// Physicists' Hermite polynomial H_n(x) by the three-term recurrence
+// H_k = 2x H_{k-1} - 2(k-1) H_{k-2} (parsmooth/linearization/_gh.py:129-151
+// builds the same coefficients).
+static double hermite(int n, double x) {
+  if (n == 0) return 1.0;
+  double h0 = 1.0, h1 = 2.0 * x;
+  for (int k = 2; k <= n; ++k) {
+    const double h2 = 2.0 * x * h1 - 2.0 * (k - 1) * h0;
+    h0 = h1;
+    h1 = h2;
+  }
+  return h1;
+}
+
+// Roots of H_p: they interlace with the roots of H_{p-1}, so each lies in one
+// bracket between consecutive roots of H_{p-1} (or the bound sqrt(2p+1));
+// bisection in each bracket.
+static void hermite_roots(int p, double* roots) {
+  double prev[SS_MAX_GH_ORDER + 1];
+  prev[0] = 0.0;
+  int np = 0;
+  for (int k = 1; k <= p; ++k) {
+    const double bound = std::sqrt(2.0 * k + 1.0) + 1.0;
+    double cur[SS_MAX_GH_ORDER + 1];
+    for (int r = 0; r < k; ++r) {
+      double lo = (r == 0) ? -bound : prev[r - 1];
+      double hi = (r == k - 1) ? bound : prev[r];
+      double flo = hermite(k, lo);
+      for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        const double fm = hermite(k, mid);
+        if (fm == 0.0) {
+          lo = hi = mid;
+          break;
+        }
+        if ((fm < 0) == (flo < 0)) {
+          lo = mid;
+          flo = fm;
+        } else {
+          hi = mid;
+        }
+      }
+      cur[r] = 0.5 * (lo + hi);
+    }
+    for (int r = 0; r < k; ++r) prev[r] = cur[r];
+    np = k;
+  }
+  for (int r = 0; r < np; ++r) roots[r] = prev[r];
+}
+
+int fill_rule(const ss_problem& p, RuleArgs& r) {
+  std::memset(&r, 0, sizeof(r));
+  r.method = p.lin_method;
+  const double n = p.nx;
+  if (p.lin_method == SS_LIN_UNSCENTED) {
+    // parsmooth/linearization/_unscented.py:64-65 (kappa default 3 + n) and :96-100
+    const double kappa = p.ut_kappa_default ? 3.0 + n : p.ut_kappa;
+    const double lam = p.ut_alpha * p.ut_alpha * (n + kappa) - n;
+    if (!(n + lam > 0)) return SS_ERR_INVALID;
+    r.ut_d[0] = std::sqrt(n + lam);
+    r.ut_d[1] = lam / (n + lam);
+    r.ut_d[2] = lam / (n + lam) + (1.0 - p.ut_alpha * p.ut_alpha + p.ut_beta);
+    r.ut_d[3] = 1.0 / (2.0 * (n + lam));
+    for (int k = 0; k < 4; ++k) r.ut_f[k] = (float)r.ut_d[k];
+  } else if (p.lin_method == SS_LIN_GAUSS_HERMITE) {
+    const int order = p.gh_order;
+    if (order < 1 || order > SS_MAX_GH_ORDER) return SS_ERR_INVALID;
+    r.gh_order = order;
+    double roots[SS_MAX_GH_ORDER];
+    hermite_roots(order, roots);
+    double fact = 1.0;
+    for (int k = 2; k <= order; ++k) fact *= k;
+    const double sqrt_pi = std::sqrt(M_PI);
+    for (int k = 0; k < order; ++k) {
+      // parsmooth/linearization/_gh.py:106-109, divided by sqrt(pi) per dimension (:120)
+      const double hp = hermite(order - 1, roots[k]);
+      const double w = std::pow(2.0, order - 1) * fact * sqrt_pi / (order * order * hp * hp);
+      r.gh_root_d[k] = std::sqrt(2.0) * roots[k];
+      r.gh_w_d[k] = w / sqrt_pi;
+      r.gh_root_f[k] = (float)r.gh_root_d[k];
+      r.gh_w_f[k] = (float)r.gh_w_d[k];
+    }
+  }
+  return SS_OK;
+}
+
+static int validate(const ss_problem* p) {
+  if (p == nullptr) return SS_ERR_INVALID;
+  if (p->dtype != SS_F32 && p->dtype != SS_F64) return SS_ERR_INVALID;
+  if (p->nx < 1 || p->ny < 1) return SS_ERR_INVALID;
+  if (p->lin_method < SS_LIN_EXTENDED || p->lin_method > SS_LIN_GAUSS_HERMITE) return SS_ERR_INVALID;
+  if (p->lin_method == SS_LIN_GAUSS_HERMITE && (p->gh_order < 1 || p->gh_order > SS_MAX_GH_ORDER))
+    return SS_ERR_INVALID;
+  if (p->batch < 1 || p->total_steps < 0 || p->max_len < 0) return SS_ERR_INVALID;
+  if (p->chunk < 0 || p->group < 0) return SS_ERR_INVALID;
+  if (p->offsets == nullptr) return SS_ERR_INVALID;
+  const ss_model* ms[2] = {&p->transition, &p->observation};
+  for (const ss_model* m : ms) {
+    if (m->noise_mean == nullptr || m->noise_chol == nullptr) return SS_ERR_INVALID;
+    if (m->kind == SS_MODEL_LINEAR && m->matrix == nullptr) return SS_ERR_INVALID;
+    if (m->kind < SS_MODEL_LINEAR || m->kind > SS_MODEL_BEARINGS) return SS_ERR_UNSUPPORTED;
+  }
+  if (find_run(p->dtype, p->nx, p->ny) == nullptr) return SS_ERR_UNSUPPORTED;
+  return SS_OK;
+}
+
+static int dispatch(Call& c) {
+  int rc = validate(c.p);
+  if (rc) return rc;
+  return find_run(c.p->dtype, c.p->nx, c.p->ny)(c);
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+int ss_version(void) { return 10000; }
+
+const char* ss_status_string(int status) {
+  switch (status) {
+    case SS_OK: return "ok";
+    case SS_ERR_INVALID: return "invalid argument";
+    case SS_ERR_UNSUPPORTED: return "unsupported model, method or dimension";
+    case SS_ERR_CUDA: return "CUDA error";
+    case SS_ERR_WORKSPACE: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+int ss_supported(const ss_problem* p) {
+  if (validate(p) != SS_OK) return 0;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_SUPPORTED;
+  c.p = p;
+  return find_run(p->dtype, p->nx, p->ny)(c) == SS_OK ? 1 : 0;
+}
+
+int ss_workspace_bytes(const ss_problem* p, size_t* bytes) {
+  if (bytes == nullptr) return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_WORKSPACE;
+  c.p = p;
+  c.ws_bytes_out = bytes;
+  return dispatch(c);
+}
+
+int ss_linearize(const ss_problem* p, int32_t which, int64_t n, const void* m, const void* chol,
+                 void* F, void* chol_out, void* b, ss_stream_t stream) {
+  if (which != 0 && which != 1) return SS_ERR_INVALID;
+  if (n < 0 || (n > 0 && (m == nullptr || chol == nullptr || F == nullptr || chol_out == nullptr || b == nullptr)))
+    return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_LINEARIZE;
+  c.p = p;
+  c.which = which;
+  c.n_points = n;
+  c.pt_m = m;
+  c.pt_L = chol;
+  c.pt_F = F;
+  c.pt_chol = chol_out;
+  c.pt_b = b;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return dispatch(c);
+}
+
+int ss_filter(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+              int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L, void* out_m,
+              void* out_L, double* out_ell, void* workspace, size_t workspace_bytes, ss_stream_t stream) {
+  if (p == nullptr || m0 == nullptr || L0 == nullptr || out_m == nullptr || out_L == nullptr) return SS_ERR_INVALID;
+  if (p->total_steps > 0 && ys == nullptr) return SS_ERR_INVALID;
+  if ((nominal_m == nullptr) != (nominal_L == nullptr)) return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_FILTER;
+  c.p = p;
+  c.ys = ys;
+  c.m0 = m0;
+  c.L0 = L0;
+  c.prior_per_sequence = prior_per_sequence;
+  c.nom_m = nominal_m;
+  c.nom_L = nominal_L;
+  c.out_m = out_m;
+  c.out_L = out_L;
+  c.out_ell = out_ell;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return dispatch(c);
+}
+
+int ss_smooth(const ss_problem* p, const void* filt_m, const void* filt_L, const void* nominal_m,
+              const void* nominal_L, void* out_m, void* out_L, void* workspace, size_t workspace_bytes,
+              ss_stream_t stream) {
+  if (p == nullptr || filt_m == nullptr || filt_L == nullptr || out_m == nullptr || out_L == nullptr)
+    return SS_ERR_INVALID;
+  if ((nominal_m == nullptr) != (nominal_L == nullptr)) return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_SMOOTH;
+  c.p = p;
+  c.in_m = filt_m;
+  c.in_L = filt_L;
+  c.nom_m = nominal_m;
+  c.nom_L = nominal_L;
+  c.out_m = out_m;
+  c.out_L = out_L;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return dispatch(c);
+}
+
+int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+                int32_t prior_per_sequence, const void* init_m, const void* init_L, int32_t n_iter,
+                double tol, void* out_m, void* out_L, double* out_ell, int32_t* out_iters,
+                uint32_t* out_flags, void* workspace, size_t workspace_bytes, ss_stream_t stream) {
+  if (p == nullptr || m0 == nullptr || L0 == nullptr || out_m == nullptr || out_L == nullptr) return SS_ERR_INVALID;
+  if (p->total_steps > 0 && ys == nullptr) return SS_ERR_INVALID;
+  if ((init_m == nullptr) != (init_L == nullptr)) return SS_ERR_INVALID;
+  if (n_iter < 0 || !(tol >= 0.0) || (tol > 0.0 && n_iter < 1)) return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_ITERATED;
+  c.p = p;
+  c.ys = ys;
+  c.m0 = m0;
+  c.L0 = L0;
+  c.prior_per_sequence = prior_per_sequence;
+  c.nom_m = init_m;
+  c.nom_L = init_L;
+  c.n_iter = n_iter;
+  c.tol = tol;
+  c.out_m = out_m;
+  c.out_L = out_L;
+  c.out_ell = out_ell;
+  c.out_iters = out_iters;
+  c.out_flags = out_flags;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return dispatch(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,11 @@
+// The (nx, ny) pairs with compiled kernels, as an X-macro list.  Each
+// instantiation file (inst_<dtype>_<nx>.cu) builds the pairs of one nx.
+#pragma once
+#define SS_FOR_DIMS(X) \
+  X(1, 1) X(1, 2) X(1, 3) \
+  X(2, 1) X(2, 2) X(2, 3) \
+  X(3, 1) X(3, 2) X(3, 3) \
+  X(4, 1) X(4, 2) X(4, 3) \
+  X(5, 1) X(5, 2) X(5, 3)
+#define SS_MAX_NX 5
+#define SS_MAX_NY 3

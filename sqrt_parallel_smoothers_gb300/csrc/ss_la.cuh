@@ -1,0 +1,309 @@
+// Small dense linear algebra for one thread: fixed-size row-major arrays that
+// the compiler keeps in registers (every loop bound is a template constant and
+// every loop is unrolled).  These are the building blocks of the per-timestep
+// element construction and of the associative-scan combines.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SS_DEV __device__ __forceinline__
+#define SS_UNROLL _Pragma("unroll")
+
+namespace ss {
+
+SS_DEV float ss_sqrt(float x) { return sqrtf(x); }
+SS_DEV double ss_sqrt(double x) { return sqrt(x); }
+SS_DEV float ss_abs(float x) { return fabsf(x); }
+SS_DEV double ss_abs(double x) { return fabs(x); }
+SS_DEV float ss_log(float x) { return logf(x); }
+SS_DEV double ss_log(double x) { return log(x); }
+SS_DEV bool ss_isfinite(float x) { return isfinite(x); }
+SS_DEV bool ss_isfinite(double x) { return isfinite(x); }
+
+// ---------------------------------------------------------------------------
+// tria: on return M[:, :ROWS] holds the lower-triangular L (diag >= 0) with
+// L L^T = M M^T (input M), and M[:, ROWS:] is zero.  Householder reflections
+// applied from the right, one per row (the transpose of QR of M^T).  This is
+// the single primitive every square-root step uses
+// (parsmooth/_utils.py:22-24 computes the same factor through jnp.linalg.qr).
+template <typename R, int ROWS, int COLS>
+SS_DEV void tria(R (&M)[ROWS][COLS]) {
+  static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
+  SS_UNROLL
+  for (int i = 0; i < ROWS; ++i) {
+    R sigma = R(0);
+    SS_UNROLL
+    for (int j = i + 1; j < COLS; ++j) sigma += M[i][j] * M[i][j];
+    const R x0 = M[i][i];
+    R beta = x0;
+    if (sigma != R(0)) {
+      const R nrm = ss_sqrt(x0 * x0 + sigma);
+      beta = (x0 <= R(0)) ? nrm : -nrm;   // opposite sign of x0: no cancellation in v0
+      const R v0 = x0 - beta;
+      const R tau = -v0 / beta;
+      const R inv = R(1) / v0;
+      R v[COLS];
+      SS_UNROLL
+      for (int j = i + 1; j < COLS; ++j) v[j] = M[i][j] * inv;
+      SS_UNROLL
+      for (int r = i + 1; r < ROWS; ++r) {
+        R w = M[r][i];
+        SS_UNROLL
+        for (int j = i + 1; j < COLS; ++j) w += M[r][j] * v[j];
+        w *= tau;
+        M[r][i] -= w;
+        SS_UNROLL
+        for (int j = i + 1; j < COLS; ++j) M[r][j] -= w * v[j];
+      }
+      SS_UNROLL
+      for (int j = i + 1; j < COLS; ++j) M[i][j] = R(0);
+    }
+    // canonical sign: non-negative diagonal (flip column i)
+    if (beta < R(0)) {
+      M[i][i] = -beta;
+      SS_UNROLL
+      for (int r = i + 1; r < ROWS; ++r) M[r][i] = -M[r][i];
+    } else {
+      M[i][i] = beta;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves against the lower-triangular N x N block of M that starts
+// at (R0, C0) (only its lower part is read).
+
+// B <- L^{-1} B   (B: N x K)
+template <typename R, int N, int K, int R0 = 0, int C0 = 0, int MR, int MC>
+SS_DEV void solve_lower(const R (&M)[MR][MC], R (&B)[N][K]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) {
+    const R inv = R(1) / M[R0 + i][C0 + i];
+    SS_UNROLL
+    for (int k = 0; k < K; ++k) {
+      R s = B[i][k];
+      SS_UNROLL
+      for (int j = 0; j < i; ++j) s -= M[R0 + i][C0 + j] * B[j][k];
+      B[i][k] = s * inv;
+    }
+  }
+}
+
+// b <- L^{-1} b
+template <typename R, int N, int R0 = 0, int C0 = 0, int MR, int MC>
+SS_DEV void solve_lower_vec(const R (&M)[MR][MC], R (&b)[N]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) {
+    R s = b[i];
+    SS_UNROLL
+    for (int j = 0; j < i; ++j) s -= M[R0 + i][C0 + j] * b[j];
+    b[i] = s / M[R0 + i][C0 + i];
+  }
+}
+
+// B <- L^{-T} B   (B: N x K)
+template <typename R, int N, int K, int R0 = 0, int C0 = 0, int MR, int MC>
+SS_DEV void solve_lower_T(const R (&M)[MR][MC], R (&B)[N][K]) {
+  SS_UNROLL
+  for (int i = N - 1; i >= 0; --i) {
+    const R inv = R(1) / M[R0 + i][C0 + i];
+    SS_UNROLL
+    for (int k = 0; k < K; ++k) {
+      R s = B[i][k];
+      SS_UNROLL
+      for (int j = i + 1; j < N; ++j) s -= M[R0 + j][C0 + i] * B[j][k];
+      B[i][k] = s * inv;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Givens: L <- tria([L, v]) for lower-triangular L (D x D) with diag >= 0.
+// Handles L == 0 (first column of a streamed factor) and zero pivots.
+template <typename R, int D>
+SS_DEV void chol_add_column(R (&L)[D][D], R (&v)[D]) {
+  SS_UNROLL
+  for (int j = 0; j < D; ++j) {
+    const R a = L[j][j];
+    const R b = v[j];
+    const R r = ss_sqrt(a * a + b * b);
+    if (r != R(0)) {
+      const R c = a / r, s = b / r;
+      L[j][j] = r;
+      SS_UNROLL
+      for (int i = j + 1; i < D; ++i) {
+        const R lij = L[i][j];
+        const R vi = v[i];
+        L[i][j] = c * lij + s * vi;
+        v[i] = c * vi - s * lij;
+      }
+    }
+  }
+}
+
+// Rank-1 update (mult = +1) or downdate (mult = -1) of a lower Cholesky
+// factor, column sweep of Algorithm 3.1 of Krause & Igel as written in
+// parsmooth/_utils.py:39-81; non-finite entries of the result become 0.
+template <typename R, int D>
+SS_DEV void chol_update(R (&L)[D][D], const R (&v)[D], R mult) {
+  R omega[D];
+  SS_UNROLL
+  for (int i = 0; i < D; ++i) omega[i] = v[i];
+  R b = R(1);
+  R out[D][D];
+  SS_UNROLL
+  for (int j = 0; j < D; ++j) {
+    const R d = L[j][j];
+    const R w = omega[j];
+    const R nd = ss_sqrt(d * d + mult / b * w * w);
+    const R gamma = d * d * b + mult * w * w;
+    const R wd = w / d;
+    SS_UNROLL
+    for (int i = j; i < D; ++i) omega[i] -= wd * L[i][j];
+    const R coef = mult * w / gamma;
+    SS_UNROLL
+    for (int i = j + 1; i < D; ++i) out[i][j] = nd * (L[i][j] / d + coef * omega[i]);
+    out[j][j] = nd;
+    b += mult * wd * wd;
+  }
+  SS_UNROLL
+  for (int i = 0; i < D; ++i) {
+    SS_UNROLL
+    for (int j = 0; j <= i; ++j) L[i][j] = ss_isfinite(out[i][j]) ? out[i][j] : R(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Products.
+
+// C = A B   (A: M x K, B: K x N)
+template <typename R, int M, int K, int N>
+SS_DEV void matmul(const R (&A)[M][K], const R (&B)[K][N], R (&C)[M][N]) {
+  SS_UNROLL
+  for (int i = 0; i < M; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) {
+      R s = R(0);
+      SS_UNROLL
+      for (int k = 0; k < K; ++k) s += A[i][k] * B[k][j];
+      C[i][j] = s;
+    }
+  }
+}
+
+// C = A^T B   (A: K x M, B: K x N)
+template <typename R, int K, int M, int N>
+SS_DEV void matmul_tn(const R (&A)[K][M], const R (&B)[K][N], R (&C)[M][N]) {
+  SS_UNROLL
+  for (int i = 0; i < M; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) {
+      R s = R(0);
+      SS_UNROLL
+      for (int k = 0; k < K; ++k) s += A[k][i] * B[k][j];
+      C[i][j] = s;
+    }
+  }
+}
+
+// y = A x
+template <typename R, int M, int N>
+SS_DEV void matvec(const R (&A)[M][N], const R (&x)[N], R (&y)[M]) {
+  SS_UNROLL
+  for (int i = 0; i < M; ++i) {
+    R s = R(0);
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) s += A[i][j] * x[j];
+    y[i] = s;
+  }
+}
+
+// y = A^T x
+template <typename R, int M, int N>
+SS_DEV void matvec_t(const R (&A)[M][N], const R (&x)[M], R (&y)[N]) {
+  SS_UNROLL
+  for (int j = 0; j < N; ++j) {
+    R s = R(0);
+    SS_UNROLL
+    for (int i = 0; i < M; ++i) s += A[i][j] * x[i];
+    y[j] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Global-memory records.  Every per-step / per-summary record is a flat array
+// of R; records are padded to a multiple of 16 bytes so that each thread moves
+// them with 16-byte vector accesses.
+
+template <typename R>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  typedef float4 type;
+  static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+  typedef double2 type;
+  static constexpr int n = 2;
+};
+
+template <typename R, int N>
+struct Padded {
+  static constexpr int n = ((N + Vec16<R>::n - 1) / Vec16<R>::n) * Vec16<R>::n;
+};
+
+// Global side must be 16-byte aligned (records sit at 16-byte multiples in a
+// 256-byte aligned workspace); the register side is copied element by element.
+SS_DEV void vec_to(const float4& v, float* d) { d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w; }
+SS_DEV void vec_to(const double2& v, double* d) { d[0] = v.x; d[1] = v.y; }
+SS_DEV float4 vec_from(const float* s) { return make_float4(s[0], s[1], s[2], s[3]); }
+SS_DEV double2 vec_from(const double* s) { return make_double2(s[0], s[1]); }
+
+template <typename R, int N>
+SS_DEV void load_rec(const R* __restrict__ src, R (&dst)[Padded<R, N>::n]) {
+  typedef typename Vec16<R>::type V;
+  constexpr int W = Vec16<R>::n;
+  const V* s = reinterpret_cast<const V*>(src);
+  SS_UNROLL
+  for (int k = 0; k < Padded<R, N>::n / W; ++k) vec_to(__ldg(s + k), dst + k * W);
+}
+
+template <typename R, int N>
+SS_DEV void store_rec(R* __restrict__ dst, const R (&src)[Padded<R, N>::n]) {
+  typedef typename Vec16<R>::type V;
+  constexpr int W = Vec16<R>::n;
+  V* d = reinterpret_cast<V*>(dst);
+  SS_UNROLL
+  for (int k = 0; k < Padded<R, N>::n / W; ++k) d[k] = vec_from(src + k * W);
+}
+
+// Copy helpers between flat records and matrices.
+template <typename R, int M, int N, int P>
+SS_DEV void unpack(const R (&rec)[P], int off, R (&A)[M][N]) {
+  SS_UNROLL
+  for (int i = 0; i < M; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) A[i][j] = rec[off + i * N + j];
+  }
+}
+template <typename R, int N, int P>
+SS_DEV void unpack_vec(const R (&rec)[P], int off, R (&a)[N]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) a[i] = rec[off + i];
+}
+template <typename R, int M, int N, int P>
+SS_DEV void pack(R (&rec)[P], int off, const R (&A)[M][N]) {
+  SS_UNROLL
+  for (int i = 0; i < M; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) rec[off + i * N + j] = A[i][j];
+  }
+}
+template <typename R, int N, int P>
+SS_DEV void pack_vec(R (&rec)[P], int off, const R (&a)[N]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) rec[off + i] = a[i];
+}
+
+}  // namespace ss

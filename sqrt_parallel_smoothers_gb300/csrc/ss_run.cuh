@@ -1,0 +1,467 @@
+// Host orchestration of one API call for a compile-time (R, NX, NY).
+#pragma once
+#include <cmath>
+#include <cstring>
+
+#include "ss_pipeline.cuh"
+
+namespace ss {
+
+enum { OP_WORKSPACE = 0, OP_LINEARIZE = 1, OP_FILTER = 2, OP_SMOOTH = 3, OP_ITERATED = 4, OP_SUPPORTED = 5 };
+
+// One entry-point call, dtype-erased.
+struct Call {
+  int op;
+  const ss_problem* p;
+  size_t* ws_bytes_out;
+  // linearize
+  int32_t which;
+  int64_t n_points;
+  const void* pt_m;
+  const void* pt_L;
+  void* pt_F;
+  void* pt_chol;
+  void* pt_b;
+  // filter / smoother / iterated
+  const void* ys;
+  const void* m0;
+  const void* L0;
+  int32_t prior_per_sequence;
+  const void* nom_m;
+  const void* nom_L;
+  const void* in_m;
+  const void* in_L;
+  void* out_m;
+  void* out_L;
+  double* out_ell;
+  int32_t n_iter;
+  double tol;
+  int32_t* out_iters;
+  uint32_t* out_flags;
+  void* ws;
+  size_t ws_bytes;
+  cudaStream_t stream;
+};
+
+typedef int (*RunFn)(const Call&);
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+struct Layout {
+  int C, G, L;
+  int64_t items[MAX_LEVELS + 1];
+  size_t lvl, lvl_stride;  // int64 [L][B+1]
+  size_t lin, selem, fT, ll, mse, active, iters, nomA_m, nomA_L, nomB_m, nomB_L;
+  size_t fsum[MAX_LEVELS + 1], fst[MAX_LEVELS + 1], ssum[MAX_LEVELS + 1], sst[MAX_LEVELS + 1];
+  size_t bytes;
+};
+
+template <typename R, int NX, int NY>
+inline int make_layout(const ss_problem& p, Layout& y) {
+  typedef Rec<R, NX, NY> Q;
+  const int64_t B = p.batch, N = p.total_steps;
+  y.C = p.chunk > 0 ? p.chunk : 16;
+  y.G = p.group > 1 ? p.group : 8;
+  const int64_t top = 4 * (int64_t)y.G;
+  int64_t n = (p.max_len + y.C - 1) / y.C;
+  y.L = 1;
+  while (n > top) {
+    n = (n + y.G - 1) / y.G;
+    ++y.L;
+    if (y.L > MAX_LEVELS) return SS_ERR_INVALID;
+  }
+  y.items[0] = N;
+  y.items[1] = (N + y.C - 1) / y.C + B;
+  for (int l = 2; l <= y.L; ++l) y.items[l] = (y.items[l - 1] + y.G - 1) / y.G + B;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o = align_up(o + bytes); return r; };
+  y.lvl_stride = (size_t)(B + 1);
+  y.lvl = take(sizeof(int64_t) * y.lvl_stride * y.L);
+  y.lin = take(sizeof(R) * Q::LIN_P * (size_t)N);
+  y.selem = take(sizeof(R) * Q::SE_P * (size_t)N);
+  for (int l = 1; l <= y.L; ++l) {
+    y.fsum[l] = take(sizeof(R) * Q::FE_P * (size_t)y.items[l]);
+    y.fst[l] = take(sizeof(R) * Q::ST_P * (size_t)y.items[l]);
+    y.ssum[l] = take(sizeof(R) * Q::SE_P * (size_t)y.items[l]);
+    y.sst[l] = take(sizeof(R) * Q::ST_P * (size_t)y.items[l]);
+  }
+  y.fT = take(sizeof(R) * Q::ST_P * (size_t)B);
+  y.ll = take(sizeof(double) * (size_t)y.items[1]);
+  y.mse = take(sizeof(double) * (size_t)B);
+  y.active = take(sizeof(int32_t) * (size_t)B);
+  y.iters = take(sizeof(int32_t) * (size_t)B);
+  const size_t S = (size_t)(N + B);
+  y.nomA_m = take(sizeof(R) * S * NX);
+  y.nomA_L = take(sizeof(R) * S * NX * NX);
+  y.nomB_m = take(sizeof(R) * S * NX);
+  y.nomB_L = take(sizeof(R) * S * NX * NX);
+  y.bytes = o;
+  return SS_OK;
+}
+
+// Host-side rule constants (unscented weights, Gauss-Hermite roots/weights).
+int fill_rule(const ss_problem& p, RuleArgs& r);
+
+template <typename R>
+inline ModelArgs<R> model_args(const ss_model& m) {
+  ModelArgs<R> a;
+  a.mat = static_cast<const R*>(m.matrix);
+  for (int k = 0; k < 4; ++k) a.p[k] = R(m.params[k]);
+  return a;
+}
+
+inline int slr_form_of(const ss_problem& p, bool fp32) {
+  if (p.slr_form == SS_SLR_DOWNDATE || p.slr_form == SS_SLR_RESIDUAL) return p.slr_form;
+  // the residual form needs a rule with identity second moment: not GH of order 1
+  if (p.lin_method == SS_LIN_GAUSS_HERMITE && p.gh_order < 2) return SS_SLR_DOWNDATE;
+  return fp32 ? SS_SLR_RESIDUAL : SS_SLR_DOWNDATE;
+}
+
+#define SS_CHECK_LAUNCH()                         \
+  do {                                            \
+    if (cudaGetLastError() != cudaSuccess) return SS_ERR_CUDA; \
+  } while (0)
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block > 0 ? (n + block - 1) / block : 1); }
+
+// Lin-kernel dispatch over the model pair and method.
+template <typename R, int NX, int NY, class TF, class OF>
+inline int launch_lin_method(const LinArgs<R>& a, int method, cudaStream_t st) {
+  const unsigned grid = grid_for(a.total, 128);
+  switch (method) {
+    case SS_LIN_EXTENDED: lin_kernel<R, NX, NY, TF, OF, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_CUBATURE: lin_kernel<R, NX, NY, TF, OF, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_UNSCENTED: lin_kernel<R, NX, NY, TF, OF, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_GAUSS_HERMITE: lin_kernel<R, NX, NY, TF, OF, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a); break;
+    default: return SS_ERR_UNSUPPORTED;
+  }
+  SS_CHECK_LAUNCH();
+  return SS_OK;
+}
+
+template <int NX>
+constexpr bool ct_ok() { return NX == 5; }
+template <int NX, int NY>
+constexpr bool bearings_ok() { return NY == 2 && NX >= 2; }
+
+template <typename R, int NX, int NY>
+inline bool models_supported(int tk, int ok) {
+  const bool t = tk == SS_MODEL_LINEAR || (tk == SS_MODEL_COORDINATED_TURN && ct_ok<NX>());
+  const bool o = ok == SS_MODEL_LINEAR || (ok == SS_MODEL_BEARINGS && bearings_ok<NX, NY>());
+  return t && o;
+}
+
+template <typename R, int NX, int NY, class TF>
+inline int launch_lin_obs(const LinArgs<R>& a, int ok, int method, cudaStream_t st) {
+  if (ok == SS_MODEL_LINEAR) return launch_lin_method<R, NX, NY, TF, LinearFn<R, NX, NY>>(a, method, st);
+  if constexpr (bearings_ok<NX, NY>()) {
+    if (ok == SS_MODEL_BEARINGS) return launch_lin_method<R, NX, NY, TF, BearingsFn<R, NX, NY>>(a, method, st);
+  }
+  return SS_ERR_UNSUPPORTED;
+}
+
+template <typename R, int NX, int NY>
+inline int launch_lin(const LinArgs<R>& a, int tk, int ok, int method, cudaStream_t st) {
+  if (a.total == 0) return SS_OK;
+  if (tk == SS_MODEL_LINEAR) return launch_lin_obs<R, NX, NY, LinearFn<R, NX, NX>>(a, ok, method, st);
+  if constexpr (ct_ok<NX>()) {
+    if (tk == SS_MODEL_COORDINATED_TURN)
+      return launch_lin_obs<R, NX, NY, CoordinatedTurnFn<R, NX, NX>>(a, ok, method, st);
+  }
+  return SS_ERR_UNSUPPORTED;
+}
+
+template <typename R, int DIN, int DOUT, class Fn>
+inline int launch_points_method(const PointArgs<R>& a, int method, cudaStream_t st) {
+  const unsigned grid = grid_for(a.n, 128);
+  switch (method) {
+    case SS_LIN_EXTENDED: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_CUBATURE: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_UNSCENTED: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_GAUSS_HERMITE: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a); break;
+    default: return SS_ERR_UNSUPPORTED;
+  }
+  SS_CHECK_LAUNCH();
+  return SS_OK;
+}
+
+// ----------------------------------------------------------------------------- runner
+
+template <typename R, int NX, int NY>
+struct Runner {
+  typedef Rec<R, NX, NY> Q;
+  const Call& c;
+  const ss_problem& p;
+  Layout y;
+  char* ws;
+  cudaStream_t st;
+  Geo geo;
+  ScanArgs<R> sa;
+  LinArgs<R> la;
+
+  explicit Runner(const Call& call) : c(call), p(*call.p), ws(static_cast<char*>(call.ws)), st(call.stream) {}
+
+  template <typename T>
+  T* at(size_t off) const { return reinterpret_cast<T*>(ws + off); }
+
+  int prepare() {
+    int rc = make_layout<R, NX, NY>(p, y);
+    if (rc) return rc;
+    if (c.ws_bytes < y.bytes || ws == nullptr) return SS_ERR_WORKSPACE;
+    geo.off = p.offsets;
+    geo.B = p.batch;
+    geo.C = y.C;
+    geo.G = y.G;
+    geo.L = y.L;
+    for (int l = 0; l <= MAX_LEVELS; ++l) geo.lvl[l] = nullptr;
+    for (int l = 1; l <= y.L; ++l) geo.lvl[l] = at<int64_t>(y.lvl) + (size_t)(l - 1) * y.lvl_stride;
+    plan_kernel<512><<<1, 512, 0, st>>>(geo, at<int64_t>(y.lvl), (int64_t)y.lvl_stride);
+    SS_CHECK_LAUNCH();
+    std::memset(&sa, 0, sizeof(sa));
+    sa.g = geo;
+    sa.ys = static_cast<const R*>(c.ys);
+    sa.lin = at<R>(y.lin);
+    sa.selem = at<R>(y.selem);
+    for (int l = 1; l <= y.L; ++l) {
+      sa.fsum[l] = at<R>(y.fsum[l]);
+      sa.fst[l] = at<R>(y.fst[l]);
+      sa.ssum[l] = at<R>(y.ssum[l]);
+      sa.sst[l] = at<R>(y.sst[l]);
+    }
+    sa.fT = at<R>(y.fT);
+    sa.m0 = static_cast<const R*>(c.m0);
+    sa.L0 = static_cast<const R*>(c.L0);
+    sa.prior_stride = c.prior_per_sequence ? 1 : 0;
+    std::memset(&la, 0, sizeof(la));
+    la.off = p.offsets;
+    la.B = p.batch;
+    la.total = p.total_steps;
+    la.tm = model_args<R>(p.transition);
+    la.om = model_args<R>(p.observation);
+    la.tq_m = static_cast<const R*>(p.transition.noise_mean);
+    la.tq_L = static_cast<const R*>(p.transition.noise_chol);
+    la.oq_m = static_cast<const R*>(p.observation.noise_mean);
+    la.oq_L = static_cast<const R*>(p.observation.noise_chol);
+    rc = fill_rule(p, la.rule);
+    if (rc) return rc;
+    la.slr_form = slr_form_of(p, sizeof(R) == 4);
+    la.out = at<R>(y.lin);
+    return SS_OK;
+  }
+
+  int lin(const R* nm, const R* nL, const int32_t* active, bool trans_only) {
+    la.nom_m = nm;
+    la.nom_L = nL;
+    la.active = active;
+    la.trans_only = trans_only ? 1 : 0;
+    return launch_lin<R, NX, NY>(la, p.transition.kind, trans_only ? SS_MODEL_LINEAR : p.observation.kind,
+                                 p.lin_method, st);
+  }
+
+  // Filter scan: level-1 summaries must already be in fsum[1] (filter_leaf).
+  int filter_scan() {
+    for (int l = 1; l < y.L; ++l) {
+      filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
+      SS_CHECK_LAUNCH();
+    }
+    filter_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    for (int l = y.L - 1; l >= 1; --l) {
+      filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
+      SS_CHECK_LAUNCH();
+    }
+    return SS_OK;
+  }
+
+  int filter_pass(bool emit_smoother) {
+    filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    int rc = filter_scan();
+    if (rc) return rc;
+    sa.emit_smoother = emit_smoother ? 1 : 0;
+    filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    return SS_OK;
+  }
+
+  int smoother_scan_and_walk() {
+    for (int l = 1; l < y.L; ++l) {
+      smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
+      SS_CHECK_LAUNCH();
+    }
+    smoother_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    for (int l = y.L - 1; l >= 1; --l) {
+      smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
+      SS_CHECK_LAUNCH();
+    }
+    smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    return SS_OK;
+  }
+
+  int run_filter() {
+    int rc = prepare();
+    if (rc) return rc;
+    rc = lin(static_cast<const R*>(c.nom_m), static_cast<const R*>(c.nom_L), nullptr, false);
+    if (rc) return rc;
+    sa.filt_m = static_cast<R*>(c.out_m);
+    sa.filt_L = static_cast<R*>(c.out_L);
+    sa.ll_chunk = c.out_ell ? at<double>(y.ll) : nullptr;
+    rc = filter_pass(false);
+    if (rc) return rc;
+    if (c.out_ell) {
+      ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, nullptr);
+      SS_CHECK_LAUNCH();
+    }
+    return SS_OK;
+  }
+
+  int run_smooth() {
+    int rc = prepare();
+    if (rc) return rc;
+    rc = lin(static_cast<const R*>(c.nom_m), static_cast<const R*>(c.nom_L), nullptr, true);
+    if (rc) return rc;
+    sa.in_m = static_cast<const R*>(c.in_m);
+    sa.in_L = static_cast<const R*>(c.in_L);
+    sa.out_m = static_cast<R*>(c.out_m);
+    sa.out_L = static_cast<R*>(c.out_L);
+    smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
+    SS_CHECK_LAUNCH();
+    return smoother_scan_and_walk();
+  }
+
+  int run_iterated() {
+    int rc = prepare();
+    if (rc) return rc;
+    const bool tol_mode = c.tol > 0.0;
+    int32_t* active = at<int32_t>(y.active);
+    int32_t* iters = at<int32_t>(y.iters);
+    double* mse = at<double>(y.mse);
+    const bool has_init = c.nom_m != nullptr;
+    init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, c.out_flags, 0);
+    SS_CHECK_LAUNCH();
+    const int calls = c.n_iter > 1 ? c.n_iter : 1;
+    R* bufm[2] = {at<R>(y.nomA_m), at<R>(y.nomB_m)};
+    R* bufL[2] = {at<R>(y.nomA_L), at<R>(y.nomB_L)};
+    const R* cur_m = static_cast<const R*>(c.nom_m);
+    const R* cur_L = static_cast<const R*>(c.nom_L);
+    int next = 0;
+    // pass 0 (init_nominal None): filter-smoother at the default nominal
+    const int first = has_init ? 1 : 0;
+    for (int k = first; k <= calls; ++k) {
+      const bool last = (k == calls);
+      const bool counted = (k >= 1);
+      R* om = last ? static_cast<R*>(c.out_m) : bufm[next];
+      R* oL = last ? static_cast<R*>(c.out_L) : bufL[next];
+      const int32_t* act = (tol_mode && counted) ? active : nullptr;
+      rc = lin(cur_m, cur_L, act, false);
+      if (rc) return rc;
+      sa.active = act;
+      sa.filt_m = nullptr;
+      sa.filt_L = nullptr;
+      sa.ll_chunk = nullptr;
+      rc = filter_pass(true);
+      if (rc) return rc;
+      sa.out_m = om;
+      sa.out_L = oL;
+      sa.prev_m = cur_m;
+      sa.prev_L = cur_L;
+      sa.mse = (tol_mode && counted) ? mse : nullptr;
+      sa.flags = last ? c.out_flags : nullptr;
+      rc = smoother_scan_and_walk();
+      if (rc) return rc;
+      if (tol_mode && counted) {
+        converge_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NX, c.tol, mse, active, iters);
+        SS_CHECK_LAUNCH();
+      }
+      cur_m = om;
+      cur_L = oL;
+      next ^= 1;
+    }
+    sa.active = nullptr;
+    sa.mse = nullptr;
+    sa.flags = nullptr;
+    if (c.out_ell) {
+      rc = lin(cur_m, cur_L, nullptr, false);
+      if (rc) return rc;
+      sa.ll_chunk = at<double>(y.ll);
+      rc = filter_pass(false);
+      if (rc) return rc;
+      ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, c.out_flags);
+      SS_CHECK_LAUNCH();
+    }
+    if (c.out_iters || (c.out_flags && tol_mode)) {
+      if (!tol_mode) {
+        init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, nullptr, calls);
+        SS_CHECK_LAUNCH();
+      }
+      finish_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, c.out_iters, c.out_flags,
+                                                                 tol_mode ? 1 : 0);
+      SS_CHECK_LAUNCH();
+    }
+    return SS_OK;
+  }
+
+  int run_linearize() {
+    PointArgs<R> a;
+    std::memset(&a, 0, sizeof(a));
+    const ss_model& mdl = c.which == 0 ? p.transition : p.observation;
+    a.n = c.n_points;
+    a.m = static_cast<const R*>(c.pt_m);
+    a.L = static_cast<const R*>(c.pt_L);
+    a.model = model_args<R>(mdl);
+    a.q_m = static_cast<const R*>(mdl.noise_mean);
+    a.q_L = static_cast<const R*>(mdl.noise_chol);
+    int rc = fill_rule(p, a.rule);
+    if (rc) return rc;
+    a.slr_form = slr_form_of(p, sizeof(R) == 4);
+    a.F = static_cast<R*>(c.pt_F);
+    a.chol = static_cast<R*>(c.pt_chol);
+    a.b = static_cast<R*>(c.pt_b);
+    if (a.n == 0) return SS_OK;
+    if (c.which == 0) {
+      if (mdl.kind == SS_MODEL_LINEAR) return launch_points_method<R, NX, NX, LinearFn<R, NX, NX>>(a, p.lin_method, st);
+      if constexpr (ct_ok<NX>()) {
+        if (mdl.kind == SS_MODEL_COORDINATED_TURN)
+          return launch_points_method<R, NX, NX, CoordinatedTurnFn<R, NX, NX>>(a, p.lin_method, st);
+      }
+    } else {
+      if (mdl.kind == SS_MODEL_LINEAR) return launch_points_method<R, NX, NY, LinearFn<R, NX, NY>>(a, p.lin_method, st);
+      if constexpr (bearings_ok<NX, NY>()) {
+        if (mdl.kind == SS_MODEL_BEARINGS)
+          return launch_points_method<R, NX, NY, BearingsFn<R, NX, NY>>(a, p.lin_method, st);
+      }
+    }
+    return SS_ERR_UNSUPPORTED;
+  }
+};
+
+template <typename R, int NX, int NY>
+int run(const Call& c) {
+  if (c.op == OP_SUPPORTED)
+    return models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind) ? SS_OK : SS_ERR_UNSUPPORTED;
+  if (!models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind)) return SS_ERR_UNSUPPORTED;
+  if (c.op == OP_WORKSPACE) {
+    Layout y;
+    const int rc = make_layout<R, NX, NY>(*c.p, y);
+    if (rc) return rc;
+    *c.ws_bytes_out = y.bytes;
+    return SS_OK;
+  }
+  Runner<R, NX, NY> r(c);
+  switch (c.op) {
+    case OP_LINEARIZE: return r.run_linearize();
+    case OP_FILTER: return r.run_filter();
+    case OP_SMOOTH: return r.run_smooth();
+    case OP_ITERATED: return r.run_iterated();
+    default: return SS_ERR_INVALID;
+  }
+}
+
+}  // namespace ss
+
+#define SS_INST(R, TAG, NX, NY) \
+  namespace ss {                \
+  int run_##TAG##_##NX##_##NY(const Call& c) { return run<R, NX, NY>(c); } \
+  }

@@ -1,0 +1,559 @@
+"""Public entry points with the signatures of ``parsmooth.methods`` (parsmooth/methods.py:14-76).
+
+Every call runs on the current CUDA device through the C ABI of
+``libsqrtsmooth.so``; each entry point is registered as a torch custom op
+(``torch.ops.sqrtsmooth.*``) so that it can be captured in CUDA graphs.
+
+Extensions over the reference:
+
+* batches of independent sequences - ``observations`` of shape ``(B, T, ny)``
+  with optional ``lengths`` (ragged, zero-padded), or packed ``(sum T_i, ny)``
+  with ``offsets``; trajectories then have ``T_i + 1`` states per sequence in
+  the same layout (padded ``(B, T+1, ...)`` or packed ``(sum (T_i+1), ...)``);
+* the dtype of ``observations`` (float32 or float64) selects the arithmetic;
+  log-likelihoods are accumulated and returned in float64.
+
+``parallel=False``, ``MVNStandard`` inputs, ``ConditionalMomentsModel`` and
+Python callables that are not device models raise ``NotImplementedError``.
+"""
+from typing import List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._base import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsModel, are_inputs_compatible
+from .linearization import resolve
+from .models import as_device_model
+
+_DT = {torch.float32: _lib.SS_F32, torch.float64: _lib.SS_F64}
+
+# ----------------------------------------------------------------------------- criteria
+
+
+class FixedIterations:
+    """Criterion ``i < n``: exactly ``n`` filter-smoother calls."""
+
+    def __init__(self, n):
+        self.n = int(n)
+
+    def __call__(self, i, *_):
+        return i < self.n
+
+
+class MeanSquaredChange:
+    """The reference default (parsmooth/methods.py:50-51): continue while the mean squared
+    change of the means exceeds ``tol``; at most ``max_iter`` calls."""
+
+    def __init__(self, tol=1e-6, max_iter=100):
+        self.tol = float(tol)
+        self.max_iter = int(max_iter)
+
+    def __call__(self, _i, prev, cur):
+        return float(torch.mean((torch.as_tensor(prev.mean) - torch.as_tensor(cur.mean)) ** 2)) > self.tol
+
+
+def _default_criterion(_i, nominal_traj_prev, curr_nominal_traj):
+    """parsmooth/methods.py:50-51."""
+    return float(torch.mean((torch.as_tensor(nominal_traj_prev.mean) -
+                             torch.as_tensor(curr_nominal_traj.mean)) ** 2)) > 1e-6
+
+
+def _criterion_schedule(criterion):
+    """``(n_calls, tol)`` for the device loop: a count criterion or the mean-squared-change test."""
+    if criterion is _default_criterion:
+        return 100, 1e-6
+    if isinstance(criterion, MeanSquaredChange):
+        return criterion.max_iter, criterion.tol
+    if isinstance(criterion, FixedIterations):
+        return max(criterion.n, 1), 0.0
+    n = 1
+    try:
+        while criterion(n, None, None):
+            n += 1
+            if n > 1_000_000:
+                raise NotImplementedError("criterion does not terminate as a function of the count")
+    except (TypeError, AttributeError) as exc:
+        raise NotImplementedError(
+            "criterion must depend only on the iteration count (e.g. `lambda i, *_: i < N`), "
+            "or be the default mean-squared-change test") from exc
+    return n, 0.0
+
+
+# ----------------------------------------------------------------------------- layout helpers
+
+
+def _device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("the square-root smoother runs on a CUDA device and none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _as(x, dtype, device):
+    return torch.as_tensor(np.asarray(x) if not isinstance(x, torch.Tensor) else x).to(
+        device=device, dtype=dtype).contiguous()
+
+
+def _lower(chol):
+    """Lower-triangular square root with the same ``L L^T`` (QR of ``chol^T`` when needed)."""
+    c = chol.detach().to("cpu", torch.float64)
+    if torch.count_nonzero(torch.triu(c, 1)) == 0:
+        return chol
+    r = torch.linalg.qr(c.transpose(-1, -2), mode="r")[1]
+    L = r.transpose(-1, -2)
+    s = torch.where(torch.diagonal(L, dim1=-2, dim2=-1) < 0, -1.0, 1.0)
+    return (L * s[..., None, :]).to(chol.dtype)
+
+
+class _Layout:
+    """Packed-batch geometry of one call and conversions to/from the user layout."""
+
+    def __init__(self, observations, lengths, offsets, dtype, device):
+        ys = observations if isinstance(observations, torch.Tensor) else torch.as_tensor(np.asarray(observations))
+        if dtype is None:
+            dtype = ys.dtype if ys.dtype in _DT else torch.float32
+        if dtype not in _DT:
+            raise TypeError(f"unsupported dtype {dtype}")
+        self.dtype, self.device = dtype, device
+        if offsets is not None:
+            if ys.ndim != 2:
+                raise ValueError("packed observations must be (sum T_i, ny)")
+            off = torch.as_tensor(offsets, dtype=torch.int64).cpu()
+            self.kind = "packed"
+            self.lengths = (off[1:] - off[:-1]).numpy()
+            self.ys = _as(ys, dtype, device)
+        elif ys.ndim == 2:
+            self.kind = "single"
+            self.lengths = np.array([ys.shape[0]], dtype=np.int64)
+            self.ys = _as(ys, dtype, device)
+        elif ys.ndim == 3:
+            self.kind = "padded"
+            B, Tm, _ = ys.shape
+            self.lengths = (np.full(B, Tm, dtype=np.int64) if lengths is None
+                            else np.asarray(torch.as_tensor(lengths).cpu(), dtype=np.int64))
+            if self.lengths.shape != (B,) or (self.lengths > Tm).any() or (self.lengths < 0).any():
+                raise ValueError("lengths must be (B,) with 0 <= T_i <= T")
+            self.Tmax = Tm
+            y = _as(ys, dtype, device)
+            self.step_idx = self._index(self.lengths, Tm, 0)
+            self.ys = y.reshape(B * Tm, -1).index_select(0, self.step_idx).contiguous()
+            self.state_idx = self._index(self.lengths, Tm + 1, 1)
+        else:
+            raise ValueError("observations must be (T, ny), (B, T, ny) or packed with offsets")
+        if (self.lengths < 0).any():
+            raise ValueError("negative sequence length")
+        self.B = int(len(self.lengths))
+        self.N = int(self.lengths.sum())
+        self.max_len = int(self.lengths.max()) if self.B else 0
+        self.ny = int(self.ys.shape[-1])
+        self.offsets = torch.as_tensor(np.concatenate([[0], np.cumsum(self.lengths)]), dtype=torch.int64,
+                                       device=device)
+
+    def _index(self, lengths, width, extra):
+        idx = [np.arange(i * width, i * width + T + extra) for i, T in enumerate(lengths)]
+        return torch.as_tensor(np.concatenate(idx) if idx else np.zeros(0, np.int64), device=self.device)
+
+    def pack_states(self, x, tail):
+        """User-layout trajectory -> packed ``(N + B, *tail)``."""
+        x = _as(x, self.dtype, self.device)
+        if self.kind == "padded":
+            return x.reshape((self.B * (self.Tmax + 1),) + tail).index_select(0, self.state_idx).contiguous()
+        return x.reshape((self.N + self.B,) + tail)
+
+    def unpack_states(self, x, tail):
+        if self.kind == "padded":
+            out = torch.zeros((self.B * (self.Tmax + 1),) + tail, dtype=x.dtype, device=x.device)
+            out.index_copy_(0, self.state_idx, x)
+            return out.reshape((self.B, self.Tmax + 1) + tail)
+        return x
+
+    def per_sequence(self, v):
+        return v[0] if self.kind == "single" else v
+
+
+def _prior(x0, lay, nx):
+    m0 = _as(x0.mean, lay.dtype, lay.device)
+    L0 = _lower(_as(x0.chol, lay.dtype, lay.device))
+    if m0.ndim == 1:
+        return m0.reshape(1, nx), L0.reshape(1, nx, nx).contiguous(), 0
+    if m0.shape[0] != lay.B:
+        raise ValueError("a per-sequence prior needs one mean per sequence")
+    L0 = L0.expand(lay.B, nx, nx) if L0.ndim == 2 else L0
+    return m0.contiguous(), L0.contiguous(), 1
+
+
+def _model_tensors(model, d_in, d_out, dtype, device, sqrt=True):
+    if isinstance(model, ConditionalMomentsModel):
+        raise NotImplementedError("ConditionalMomentsModel is not supported by the GPU smoother")
+    if not isinstance(model, FunctionalModel):
+        raise TypeError(f"expected a FunctionalModel, got {type(model).__name__}")
+    fn = as_device_model(model.function)
+    if fn.d_out != d_out or fn.d_in != d_in:
+        raise ValueError(f"{fn!r} maps R^{fn.d_in} -> R^{fn.d_out}, expected R^{d_in} -> R^{d_out}")
+    q = model.mvn
+    if isinstance(q, MVNStandard):
+        raise NotImplementedError("covariance-form (MVNStandard) models are not supported: use MVNSqrt")
+    qm = _as(q.mean, dtype, device).reshape(d_out)
+    qL = _lower(_as(q.chol, dtype, device)).reshape(d_out, d_out).contiguous()
+    mat = fn.matrix()
+    mat = None if mat is None else _as(mat, dtype, device)
+    return fn, mat, qm, qL
+
+
+def _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, extra):
+    p = method.params
+    kappa_default = 1 if p.get("kappa", None) is None else 0
+    return [nx, ny, method.code, kappa_default, int(p.get("order", 3)), int(slr_form), int(chunk), int(group),
+            fn_t.kind, fn_o.kind, lay.B, lay.N, lay.max_len] + list(extra)
+
+
+def _fcfg(method, fn_t, fn_o, extra=()):
+    p = method.params
+    kappa = p.get("kappa", None)
+    return [float(p.get("alpha", 1.0)), float(p.get("beta", 0.0)), float(0.0 if kappa is None else kappa)] + \
+        [float(v) for v in fn_t.params()] + [float(v) for v in fn_o.params()] + [float(v) for v in extra]
+
+
+# ----------------------------------------------------------------------------- ctypes glue
+
+_WS = {}
+
+
+def _workspace(nbytes, device):
+    key = (device.index, torch.cuda.current_stream(device).cuda_stream)
+    buf = _WS.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        _WS[key] = buf
+    return buf
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def _problem(icfg, fcfg, dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL):
+    (nx, ny, code, kdef, order, slr, chunk, group, tk, ok, B, N, maxlen) = icfg[:13]
+    pr = _lib.SSProblem()
+    pr.dtype = _DT[dtype]
+    pr.nx, pr.ny, pr.lin_method = nx, ny, code
+    pr.ut_alpha, pr.ut_beta, pr.ut_kappa = fcfg[0], fcfg[1], fcfg[2]
+    pr.ut_kappa_default, pr.gh_order, pr.slr_form = kdef, order, slr
+    pr.chunk, pr.group = chunk, group
+    for mdl, kind, mat, qm, qL, par in ((pr.transition, tk, t_mat, t_qm, t_qL, fcfg[3:7]),
+                                        (pr.observation, ok, o_mat, o_qm, o_qL, fcfg[7:11])):
+        mdl.kind = kind
+        mdl.matrix = _ptr(mat)
+        for k in range(4):
+            mdl.params[k] = par[k]
+        mdl.noise_mean = _ptr(qm)
+        mdl.noise_chol = _ptr(qL)
+    pr.batch, pr.total_steps, pr.max_len = B, N, maxlen
+    pr.offsets = _ptr(offsets)
+    return pr
+
+
+def _ws_for(pr, device):
+    lib = _lib.load()
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.ss_workspace_bytes(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
+    return _workspace(nbytes.value, device), nbytes.value
+
+
+def _stream(device):
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+# ----------------------------------------------------------------------------- torch ops
+
+@torch.library.custom_op("sqrtsmooth::filter", mutates_args=())
+def _filter_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L0: torch.Tensor,
+               nom_m: Optional[torch.Tensor], nom_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor],
+               t_qm: torch.Tensor, t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor,
+               o_qL: torch.Tensor, icfg: List[int], fcfg: List[float]
+               ) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    nx, B, N = icfg[0], icfg[10], icfg[11]
+    prior_per_seq, want_ell = icfg[13], icfg[14]
+    dev = ys.device
+    pr = _problem(icfg, fcfg, ys.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    ws, nbytes = _ws_for(pr, dev)
+    out_m = torch.empty((N + B, nx), dtype=ys.dtype, device=dev)
+    out_L = torch.empty((N + B, nx, nx), dtype=ys.dtype, device=dev)
+    ell = torch.empty((B if want_ell else 0,), dtype=torch.float64, device=dev)
+    _lib.check(_lib.load().ss_filter(_lib.ctypes.byref(pr), _ptr(ys), _ptr(m0), _ptr(L0), prior_per_seq,
+                                     _ptr(nom_m), _ptr(nom_L), _ptr(out_m), _ptr(out_L),
+                                     _ptr(ell) if want_ell else None, _ptr(ws), nbytes, _stream(dev)))
+    return out_m, out_L, ell
+
+
+@_filter_op.register_fake
+def _(ys, offsets, m0, L0, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg):
+    nx, B, N = icfg[0], icfg[10], icfg[11]
+    return (ys.new_empty((N + B, nx)), ys.new_empty((N + B, nx, nx)),
+            ys.new_empty((B if icfg[14] else 0,), dtype=torch.float64))
+
+
+@torch.library.custom_op("sqrtsmooth::smooth", mutates_args=())
+def _smooth_op(filt_m: torch.Tensor, filt_L: torch.Tensor, offsets: torch.Tensor, nom_m: Optional[torch.Tensor],
+               nom_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor], t_qm: torch.Tensor,
+               t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor, o_qL: torch.Tensor,
+               icfg: List[int], fcfg: List[float]) -> Tuple[torch.Tensor, torch.Tensor]:
+    dev = filt_m.device
+    pr = _problem(icfg, fcfg, filt_m.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    ws, nbytes = _ws_for(pr, dev)
+    out_m = torch.empty_like(filt_m)
+    out_L = torch.empty_like(filt_L)
+    _lib.check(_lib.load().ss_smooth(_lib.ctypes.byref(pr), _ptr(filt_m), _ptr(filt_L), _ptr(nom_m),
+                                     _ptr(nom_L), _ptr(out_m), _ptr(out_L), _ptr(ws), nbytes, _stream(dev)))
+    return out_m, out_L
+
+
+@_smooth_op.register_fake
+def _(filt_m, filt_L, offsets, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg):
+    return torch.empty_like(filt_m), torch.empty_like(filt_L)
+
+
+@torch.library.custom_op("sqrtsmooth::iterated", mutates_args=())
+def _iterated_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L0: torch.Tensor,
+                 init_m: Optional[torch.Tensor], init_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor],
+                 t_qm: torch.Tensor, t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor,
+                 o_qL: torch.Tensor, icfg: List[int], fcfg: List[float]
+                 ) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor]:
+    nx, B, N = icfg[0], icfg[10], icfg[11]
+    prior_per_seq, want_ell, n_iter = icfg[13], icfg[14], icfg[15]
+    tol = fcfg[11]
+    dev = ys.device
+    pr = _problem(icfg, fcfg, ys.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    ws, nbytes = _ws_for(pr, dev)
+    out_m = torch.empty((N + B, nx), dtype=ys.dtype, device=dev)
+    out_L = torch.empty((N + B, nx, nx), dtype=ys.dtype, device=dev)
+    ell = torch.empty((B if want_ell else 0,), dtype=torch.float64, device=dev)
+    iters = torch.empty((B,), dtype=torch.int32, device=dev)
+    flags = torch.empty((B,), dtype=torch.int32, device=dev)
+    _lib.check(_lib.load().ss_iterated(_lib.ctypes.byref(pr), _ptr(ys), _ptr(m0), _ptr(L0), prior_per_seq,
+                                       _ptr(init_m), _ptr(init_L), n_iter, tol, _ptr(out_m), _ptr(out_L),
+                                       _ptr(ell) if want_ell else None, _ptr(iters), _ptr(flags), _ptr(ws),
+                                       nbytes, _stream(dev)))
+    return out_m, out_L, ell, iters, flags
+
+
+@_iterated_op.register_fake
+def _(ys, offsets, m0, L0, init_m, init_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg):
+    nx, B, N = icfg[0], icfg[10], icfg[11]
+    return (ys.new_empty((N + B, nx)), ys.new_empty((N + B, nx, nx)),
+            ys.new_empty((B if icfg[14] else 0,), dtype=torch.float64),
+            ys.new_empty((B,), dtype=torch.int32), ys.new_empty((B,), dtype=torch.int32))
+
+
+@torch.library.custom_op("sqrtsmooth::linearize", mutates_args=())
+def _linearize_op(m: torch.Tensor, L: torch.Tensor, offsets: torch.Tensor, t_mat: Optional[torch.Tensor],
+                  t_qm: torch.Tensor, t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor,
+                  o_qL: torch.Tensor, icfg: List[int], fcfg: List[float], which: int
+                  ) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    nx, ny = icfg[0], icfg[1]
+    d_out = nx if which == 0 else ny
+    n = m.shape[0]
+    dev = m.device
+    pr = _problem(icfg, fcfg, m.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    F = torch.empty((n, d_out, nx), dtype=m.dtype, device=dev)
+    chol = torch.empty((n, d_out, d_out), dtype=m.dtype, device=dev)
+    b = torch.empty((n, d_out), dtype=m.dtype, device=dev)
+    _lib.check(_lib.load().ss_linearize(_lib.ctypes.byref(pr), which, n, _ptr(m), _ptr(L), _ptr(F), _ptr(chol),
+                                        _ptr(b), _stream(dev)))
+    return F, chol, b
+
+
+@_linearize_op.register_fake
+def _(m, L, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg, which):
+    nx, ny = icfg[0], icfg[1]
+    d_out = nx if which == 0 else ny
+    n = m.shape[0]
+    return m.new_empty((n, d_out, nx)), m.new_empty((n, d_out, d_out)), m.new_empty((n, d_out))
+
+
+# ----------------------------------------------------------------------------- public API
+
+def _check_common(x0, parallel, method):
+    if not parallel:
+        raise NotImplementedError("only parallel=True is implemented on the GPU")
+    if isinstance(x0, MVNStandard):
+        raise NotImplementedError("covariance-form (MVNStandard) inputs are not supported: use MVNSqrt")
+    if not isinstance(x0, MVNSqrt):
+        raise TypeError(f"x0 must be an MVNSqrt, got {type(x0).__name__}")
+    return resolve(method)
+
+
+def _nominal(nominal, lay, nx):
+    if nominal is None:
+        return None, None
+    if isinstance(nominal, MVNStandard):
+        raise NotImplementedError("covariance-form nominal trajectories are not supported")
+    m = lay.pack_states(nominal.mean, (nx,))
+    L = lay.pack_states(nominal.chol, (nx, nx))
+    return m, _lower_batched(L)
+
+
+def _lower_batched(L):
+    if torch.count_nonzero(torch.triu(L, 1)) == 0:
+        return L.contiguous()
+    return _lower(L).to(L.device).contiguous()
+
+
+def _dummy_observation(nx, dtype, device):
+    from .models import LinearModel
+    fn = LinearModel(torch.zeros(1, nx))
+    return fn, _as(fn.A, dtype, device), torch.zeros(1, dtype=dtype, device=device), \
+        torch.ones(1, 1, dtype=dtype, device=device)
+
+
+def filtering(observations, x0, transition_model, observation_model, linearization_method,
+              nominal_trajectory=None, parallel=True, return_loglikelihood=False, *, lengths=None,
+              offsets=None, chunk=0, group=0, slr_form=0):
+    """Parallel square-root filter (parsmooth/methods.py:14-26 -> parsmooth/parallel/_filtering.py:13-61)."""
+    method = _check_common(x0, parallel, linearization_method)
+    if nominal_trajectory is not None:
+        are_inputs_compatible(x0, nominal_trajectory)
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_qL = _model_tensors(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, L0, per = _prior(x0, lay, nx)
+    nm, nL = _nominal(nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, slr_form,
+                 [per, int(bool(return_loglikelihood))])
+    out_m, out_L, ell = torch.ops.sqrtsmooth.filter(lay.ys, lay.offsets, m0, L0, nm, nL, t_mat, t_qm, t_qL,
+                                                    o_mat, o_qm, o_qL, icfg, _fcfg(method, fn_t, fn_o))
+    res = MVNSqrt(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_L, (nx, nx)))
+    if return_loglikelihood:
+        return res, lay.per_sequence(ell)
+    return res
+
+
+def smoothing(transition_model, filter_trajectory, linearization_method, nominal_trajectory=None,
+              parallel=True, *, lengths=None, offsets=None, chunk=0, group=0, slr_form=0):
+    """Parallel square-root RTS smoother (parsmooth/methods.py:29-35 -> parsmooth/parallel/_smoothing.py:14-44).
+
+    For batches pass ``lengths`` (padded trajectories ``(B, T+1, ...)``) or
+    ``offsets`` (packed trajectories, offsets of the steps)."""
+    method = _check_common(filter_trajectory, parallel, linearization_method)
+    if nominal_trajectory is not None:
+        are_inputs_compatible(filter_trajectory, nominal_trajectory)
+    dev = _device()
+    fm = torch.as_tensor(filter_trajectory.mean) if not isinstance(filter_trajectory.mean, torch.Tensor) \
+        else filter_trajectory.mean
+    nx = int(fm.shape[-1])
+    dtype = fm.dtype if fm.dtype in _DT else torch.float32
+    # geometry from the trajectory shape: T+1 states per sequence
+    if offsets is not None:
+        off = torch.as_tensor(offsets, dtype=torch.int64)
+        n_steps = int(off[-1])
+        fake = torch.zeros((n_steps, 1), dtype=dtype)
+        lay = _Layout(fake, None, off, dtype, dev)
+    elif fm.ndim == 2:
+        lay = _Layout(torch.zeros((fm.shape[0] - 1, 1), dtype=dtype), None, None, dtype, dev)
+    else:
+        B, Tp1 = fm.shape[:2]
+        lay = _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev)
+    fmp = lay.pack_states(filter_trajectory.mean, (nx,))
+    fLp = _lower_batched(lay.pack_states(filter_trajectory.chol, (nx, nx)))
+    nm, nL = _nominal(nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, 1, fn_t, fn_o, lay, chunk, group, slr_form, [0, 0])
+    out_m, out_L = torch.ops.sqrtsmooth.smooth(fmp, fLp, lay.offsets, nm, nL, t_mat, t_qm, t_qL, o_mat, o_qm,
+                                               o_qL, icfg, _fcfg(method, fn_t, fn_o))
+    return MVNSqrt(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_L, (nx, nx)))
+
+
+def filter_smoother(observations, x0, transition_model, observation_model, linearization_method,
+                    nominal_trajectory=None, parallel=True, **kw):
+    """parsmooth/methods.py:38-47."""
+    filt = filtering(observations, x0, transition_model, observation_model, linearization_method,
+                     nominal_trajectory, parallel, **kw)
+    kw = {k: v for k, v in kw.items() if k in ("lengths", "offsets", "chunk", "group", "slr_form")}
+    return smoothing(transition_model, filt, linearization_method, nominal_trajectory, parallel, **kw)
+
+
+def iterated_smoothing(observations, x0, transition_model, observation_model, linearization_method,
+                       init_nominal_trajectory=None, parallel=True, criterion=_default_criterion,
+                       return_loglikelihood=False, *, lengths=None, offsets=None, chunk=0, group=0,
+                       slr_form=0, return_info=False):
+    """Iterated square-root smoother (parsmooth/methods.py:54-76), the whole loop on the device.
+
+    ``criterion`` may be a count test such as ``lambda i, *_: i < N`` (exactly
+    ``N`` filter-smoother calls), the default mean-squared-change test, or
+    :class:`MeanSquaredChange` / :class:`FixedIterations`.  With
+    ``return_info=True`` a dict with per-sequence ``iterations`` and status
+    ``flags`` (1 non-finite output, 2 non-finite log-likelihood, 4 not
+    converged) is returned last."""
+    method = _check_common(x0, parallel, linearization_method)
+    if init_nominal_trajectory is not None:
+        are_inputs_compatible(x0, init_nominal_trajectory)
+    n_calls, tol = _criterion_schedule(criterion)
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_qL = _model_tensors(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, L0, per = _prior(x0, lay, nx)
+    im, iL = _nominal(init_nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, slr_form,
+                 [per, int(bool(return_loglikelihood)), n_calls])
+    fcfg = _fcfg(method, fn_t, fn_o, [tol])
+    out_m, out_L, ell, iters, flags = torch.ops.sqrtsmooth.iterated(lay.ys, lay.offsets, m0, L0, im, iL, t_mat,
+                                                                    t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg)
+    res = MVNSqrt(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_L, (nx, nx)))
+    out = (res,)
+    if return_loglikelihood:
+        out += (lay.per_sequence(ell),)
+    if return_info:
+        out += ({"iterations": lay.per_sequence(iters), "flags": lay.per_sequence(flags)},)
+    return out[0] if len(out) == 1 else out
+
+
+def linearize(model, x, method):
+    """Linearise ``model`` at ``x`` (one point or a batch) with ``method`` on the GPU.
+
+    Equivalent of ``method(model, x)`` in parsmooth/linearization/*.py."""
+    method = resolve(method)
+    if isinstance(x, MVNStandard):
+        raise NotImplementedError("covariance-form inputs are not supported: use MVNSqrt")
+    dev = _device()
+    m = torch.as_tensor(x.mean) if not isinstance(x.mean, torch.Tensor) else x.mean
+    dtype = m.dtype if m.dtype in _DT else torch.float32
+    single = m.ndim == 1
+    nx = int(m.shape[-1])
+    mm = _as(m, dtype, dev).reshape(-1, nx)
+    LL = _lower_batched(_as(x.chol, dtype, dev).reshape(-1, nx, nx))
+    fn = as_device_model(model.function)
+    d_out = fn.d_out
+    is_obs = not (d_out == nx and fn.kind != _lib.SS_MODEL_BEARINGS)
+    fnm, mat, qm, qL = _model_tensors(model, nx, d_out, dtype, dev)
+    if is_obs:
+        fn_t, t_mat, t_qm, t_qL = _dummy_transition(nx, dtype, dev)
+        o = (fnm, mat, qm, qL)
+        ny = d_out
+    else:
+        fn_t, t_mat, t_qm, t_qL = fnm, mat, qm, qL
+        o = _dummy_observation(nx, dtype, dev)
+        ny = 1
+    lay_off = torch.zeros(2, dtype=torch.int64, device=dev)
+
+    class _L:
+        B, N, max_len = 1, 0, 0
+
+    icfg = _icfg(method, nx, ny, fn_t, o[0], _L, 0, 0, 0, [])
+    F, chol, b = torch.ops.sqrtsmooth.linearize(mm, LL, lay_off, t_mat, t_qm, t_qL, o[1], o[2], o[3], icfg,
+                                                _fcfg(method, fn_t, o[0]), 1 if is_obs else 0)
+    if single:
+        return F[0], chol[0], b[0]
+    return F.reshape(m.shape[:-1] + F.shape[1:]), chol.reshape(m.shape[:-1] + chol.shape[1:]), \
+        b.reshape(m.shape[:-1] + b.shape[1:])
+
+
+def _dummy_transition(nx, dtype, device):
+    from .models import LinearModel
+    fn = LinearModel(torch.eye(nx))
+    return fn, _as(fn.A, dtype, device), torch.zeros(nx, dtype=dtype, device=device), \
+        torch.eye(nx, dtype=dtype, device=device)

@@ -1,0 +1,263 @@
+"""GPU parity against the FP64 oracle, through the C ABI (via the torch ops).
+
+Tolerances (norm-wise relative, see ``_parity.assert_rel``): FP64 runs 1e-10
+(1e-9 for iterated nonlinear runs, whose fixed point amplifies rounding);
+FP32 runs 2e-4 on the reference's small random systems.
+"""
+import functools
+
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import sqrt_parallel_smoothers_gb300 as S
+from tests._parity import (GPU_LIN, ORACLE_LIN, assert_rel, bearings_pair, cov, linear_pair, np_)
+from tests._systems import get_system, lgssm
+
+pytestmark = pytest.mark.gpu
+
+F64_TOL = 1e-10
+F32_TOL = 2e-4
+
+
+def _tol(dtype):
+    return F64_TOL if dtype == torch.float64 else F32_TOL
+
+
+# ----------------------------------------------------------------------------- linearisation
+
+@pytest.mark.parametrize("method", list(GPU_LIN))
+@pytest.mark.parametrize("dims", [(1, 1), (2, 3), (3, 2), (4, 2), (5, 3)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_linearize_linear(method, dims, dtype):
+    nx, ny = dims
+    rng = np.random.RandomState(nx * 10 + ny)
+    A = rng.randn(ny, nx)
+    c = rng.randn(ny)
+    cR = np.tril(rng.rand(ny, ny)) + 0.1 * np.eye(ny)
+    om, gm = linear_pair(A, c, cR)
+    m = rng.randn(7, nx)
+    L = np.tril(rng.rand(7, nx, nx)) + 0.5 * np.eye(nx)
+    Fo, Lo, bo = ORACLE_LIN[method](om, O.MVNSqrt(m, L))
+    Fg, Lg, bg = S.linearize(gm, S.MVNSqrt(torch.as_tensor(m, dtype=dtype), torch.as_tensor(L, dtype=dtype)),
+                             GPU_LIN[method])
+    tol = 1e-10 if dtype == torch.float64 else 1e-4
+    assert_rel(Fg, Fo, tol, "F")
+    assert_rel(bg, bo, tol, "b")
+    assert_rel(cov(Lg), cov(Lo), tol, "LL^T")
+
+
+@pytest.mark.parametrize("method", list(GPU_LIN))
+@pytest.mark.parametrize("which", ["transition", "observation"])
+def test_linearize_bearings_models_fp64(method, which):
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    rng = np.random.RandomState(1)
+    m = rng.randn(9, 5) + np.array([0.5, 0.5, 1.0, 0.0, 1.0])
+    L = 0.3 * (np.tril(rng.rand(9, 5, 5)) + np.eye(5))
+    om_, gm_ = (ot, gt) if which == "transition" else (oo, go)
+    Fo, Lo, bo = ORACLE_LIN[method](om_, O.MVNSqrt(m, L))
+    Fg, Lg, bg = S.linearize(gm_, S.MVNSqrt(torch.as_tensor(m), torch.as_tensor(L)), GPU_LIN[method])
+    assert_rel(Fg, Fo, 1e-10, "F")
+    assert_rel(bg, bo, 1e-10, "b")
+    # the downdate of the reference loses ~1e-16 * |Phi| absolutely; compare the covariance
+    assert_rel(cov(Lg), cov(Lo), 1e-10, "LL^T")
+
+
+def test_linearize_unscented_and_gh_parameters():
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    rng = np.random.RandomState(2)
+    m = rng.randn(4, 5)
+    L = 0.2 * (np.tril(rng.rand(4, 5, 5)) + np.eye(5))
+    for o_m, g_m in [(O.linearization.Unscented(0.8, 2.0, 1.0), functools.partial(S.linearization.unscented,
+                                                                                  alpha=0.8, beta=2.0, kappa=1.0)),
+                     (O.linearization.GaussHermite(4), functools.partial(S.linearization.gauss_hermite, order=4))]:
+        Fo, Lo, bo = o_m(oo, O.MVNSqrt(m, L))
+        Fg, Lg, bg = S.linearize(go, S.MVNSqrt(torch.as_tensor(m), torch.as_tensor(L)), g_m)
+        assert_rel(Fg, Fo, 1e-10, "F")
+        assert_rel(bg, bo, 1e-10, "b")
+        assert_rel(cov(Lg), cov(Lo), 1e-10, "LL^T")
+
+
+# ----------------------------------------------------------------------------- filter / smoother
+
+def _system(dim_x, dim_y, seed, T=10):
+    s = lgssm(dim_x, dim_y, T, seed)
+    (ot, gt) = linear_pair(s["F"], s["b"], s["cholQ"])
+    (oo, go) = linear_pair(s["H"], s["c"], s["cholR"])
+    return s, (ot, oo), (gt, go)
+
+
+@pytest.mark.parametrize("dim_x", [1, 2, 3])
+@pytest.mark.parametrize("dim_y", [1, 2, 3])
+@pytest.mark.parametrize("seed", [0, 42])
+@pytest.mark.parametrize("method", ["cubature", "extended"])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_filter_vs_oracle(dim_x, dim_y, seed, method, dtype):
+    s, (ot, oo), (gt, go) = _system(dim_x, dim_y, seed)
+    T = s["ys"].shape[0]
+    nom_m = s["m_nominal"]
+    nom_L = np.repeat(np.eye(dim_x)[None], T + 1, 0)
+    ref, ref_ell = O.methods.filtering(s["ys"].astype(float), s["chol_x0"], ot, oo, ORACLE_LIN[method],
+                                       O.MVNSqrt(nom_m, nom_L), True, return_loglikelihood=True)
+    seq = O.sequential.filtering(s["ys"].astype(float), s["chol_x0"], ot, oo, ORACLE_LIN[method],
+                                 O.MVNSqrt(nom_m, nom_L))
+    x0 = S.MVNSqrt(torch.as_tensor(s["chol_x0"].mean), torch.as_tensor(s["chol_x0"].chol))
+    res, ell = S.filtering(torch.as_tensor(s["ys"], dtype=dtype), x0, gt, go, GPU_LIN[method],
+                           S.MVNSqrt(torch.as_tensor(nom_m), torch.as_tensor(nom_L)), return_loglikelihood=True)
+    tol = _tol(dtype)
+    assert_rel(res.mean, ref.mean, tol, "mean")
+    assert_rel(cov(res.chol), cov(ref.chol), tol, "cov")
+    assert_rel(res.mean, seq.mean, tol, "mean vs sequential")
+    assert abs(float(ell) - ref_ell) <= tol * max(1.0, abs(ref_ell))
+
+
+@pytest.mark.parametrize("dim_x", [1, 2, 3])
+@pytest.mark.parametrize("dim_y", [1, 3])
+@pytest.mark.parametrize("method", ["cubature", "extended"])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_smoother_vs_oracle(dim_x, dim_y, method, dtype):
+    s, (ot, oo), (gt, go) = _system(dim_x, dim_y, 0)
+    ys = s["ys"].astype(float)
+    filt = O.sequential.filtering(ys, s["chol_x0"], ot, oo, ORACLE_LIN[method])
+    ref = O.methods.smoothing(ot, filt, ORACLE_LIN[method])
+    res = S.smoothing(gt, S.MVNSqrt(torch.as_tensor(filt.mean, dtype=dtype), torch.as_tensor(filt.chol, dtype=dtype)),
+                      GPU_LIN[method])
+    tol = _tol(dtype)
+    assert_rel(res.mean, ref.mean, tol, "mean")
+    assert_rel(cov(res.chol), cov(ref.chol), tol, "cov")
+
+
+@pytest.mark.parametrize("dim_x", [1, 2])
+@pytest.mark.parametrize("dim_y", [1, 2])
+@pytest.mark.parametrize("method", ["cubature", "extended"])
+def test_iterated_linear_vs_oracle(dim_x, dim_y, method):
+    s, (ot, oo), (gt, go) = _system(dim_x, dim_y, 0, T=5)
+    ys = s["ys"].astype(float)
+    nom = (s["m_nominal"], np.repeat(np.eye(dim_x)[None], 6, 0))
+    ref = O.methods.iterated_smoothing(ys, s["chol_x0"], ot, oo, ORACLE_LIN[method], O.MVNSqrt(*nom), True,
+                                       criterion=lambda i, *_: i < 5)
+    x0 = S.MVNSqrt(torch.as_tensor(s["chol_x0"].mean), torch.as_tensor(s["chol_x0"].chol))
+    res = S.iterated_smoothing(torch.as_tensor(ys), x0, gt, go, GPU_LIN[method],
+                               S.MVNSqrt(torch.as_tensor(nom[0]), torch.as_tensor(nom[1])),
+                               criterion=lambda i, *_: i < 5)
+    assert_rel(res.mean, ref.mean, 1e-10, "mean")
+    assert_rel(cov(res.chol), cov(ref.chol), 1e-10, "cov")
+
+
+# ----------------------------------------------------------------------------- scan geometry
+
+@pytest.mark.parametrize("T", [1, 2, 3, 7, 64, 1000])
+@pytest.mark.parametrize("chunk,group", [(1, 2), (3, 2), (16, 8), (5, 3)])
+def test_cv_geometry_fp64(T, chunk, group):
+    """Constant-velocity model at many chunk/group sizes (multi-level scans) vs the oracle."""
+    w = S.data.cv_workload(T, seed=0)
+    cQ, cR = np.linalg.cholesky(w["Q"]), np.linalg.cholesky(w["R"])
+    ot, gt = linear_pair(w["F"], np.zeros(4), cQ)
+    oo, go = linear_pair(w["H"], np.zeros(2), cR)
+    ys = w["ys"].astype(float)
+    ref, ref_ell = O.methods.filtering(ys, O.MVNSqrt(w["m0"], w["P0"]), ot, oo, O.linearization.extended,
+                                       None, True, return_loglikelihood=True)
+    sm = O.methods.smoothing(ot, ref, O.linearization.extended)
+    x0 = S.MVNSqrt(torch.as_tensor(w["m0"]), torch.as_tensor(w["P0"]))
+    res, ell = S.filtering(torch.as_tensor(ys), x0, gt, go, S.linearization.extended, return_loglikelihood=True,
+                           chunk=chunk, group=group)
+    assert_rel(res.mean, ref.mean, F64_TOL, "filtered mean")
+    assert_rel(cov(res.chol), cov(ref.chol), F64_TOL, "filtered cov")
+    assert abs(float(ell) - ref_ell) <= F64_TOL * abs(ref_ell)
+    sres = S.smoothing(gt, res, S.linearization.extended, chunk=chunk, group=group)
+    assert_rel(sres.mean, sm.mean, F64_TOL, "smoothed mean")
+    assert_rel(cov(sres.chol), cov(sm.chol), F64_TOL, "smoothed cov")
+    it = S.iterated_smoothing(torch.as_tensor(ys), x0, gt, go, S.linearization.extended, None,
+                              criterion=lambda i, *_: i < 1, chunk=chunk, group=group)
+    assert_rel(it.mean, O.methods.filter_smoother(ys, O.MVNSqrt(w["m0"], w["P0"]), ot, oo,
+                                                  O.linearization.extended,
+                                                  O.methods.filter_smoother(ys, O.MVNSqrt(w["m0"], w["P0"]), ot, oo,
+                                                                            O.linearization.extended)).mean,
+               F64_TOL, "iterated")
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_ragged_batch_vs_oracle(dtype):
+    lengths = np.array([0, 1, 2, 7, 33, 100, 5, 64])
+    B = len(lengths)
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    batch = S.data.bearings_batch(lengths)
+    m0 = S.data.BEARINGS_M0
+    Tm = int(lengths.max())
+    ys_pad = np.zeros((B, Tm, 2))
+    for i, T in enumerate(lengths):
+        ys_pad[i, :T] = batch["ys"][batch["offsets"][i]:batch["offsets"][i + 1]]
+    x0 = S.MVNSqrt(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64))
+    res, ell, info = S.iterated_smoothing(torch.as_tensor(ys_pad, dtype=dtype), x0, gt, go,
+                                          S.linearization.cubature, None, criterion=lambda i, *_: i < 3,
+                                          return_loglikelihood=True, lengths=lengths, return_info=True,
+                                          chunk=4, group=2)
+    tol = 1e-9 if dtype == torch.float64 else 5e-3
+    for i, T in enumerate(lengths):
+        ref, ref_ell = O.methods.iterated_smoothing(ys_pad[i, :T], O.MVNSqrt(m0, np.eye(5)), ot, oo,
+                                                    O.linearization.cubature, None, True,
+                                                    criterion=lambda k, *_: k < 3, return_loglikelihood=True)
+        assert_rel(res.mean[i, :T + 1], ref.mean, tol, f"seq {i} mean")
+        assert_rel(cov(res.chol[i, :T + 1]), cov(ref.chol), tol, f"seq {i} cov")
+        if T > 0:
+            assert abs(float(ell[i]) - ref_ell) <= tol * max(1.0, abs(ref_ell)), (i, float(ell[i]), ref_ell)
+    assert int(info["iterations"][0]) == 3
+    assert int(info["flags"].abs().sum()) == 0
+
+
+def test_default_criterion_matches_oracle():
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    w = S.data.bearings_workload(200, seed=3)
+    ys = w["ys"].astype(float)
+    x0o = O.MVNSqrt(w["m0"], np.eye(5))
+    nom = (np.repeat(w["m0"][None], 201, 0), np.repeat(np.eye(5)[None], 201, 0))
+    n_calls = []
+
+    def crit(i, prev, cur):
+        go_on = O.methods.default_criterion(i, prev, cur)
+        n_calls.append(i)
+        return go_on
+
+    ref = O.methods.iterated_smoothing(ys, x0o, ot, oo, O.linearization.extended, O.MVNSqrt(*nom), True,
+                                       criterion=crit)
+    res, info = S.iterated_smoothing(torch.as_tensor(ys), S.MVNSqrt(torch.as_tensor(w["m0"]), torch.eye(5,
+                                     dtype=torch.float64)), gt, go, S.linearization.extended,
+                                     S.MVNSqrt(torch.as_tensor(nom[0]), torch.as_tensor(nom[1])), return_info=True)
+    assert int(info["iterations"]) == max(n_calls)
+    assert_rel(res.mean, ref.mean, 1e-8, "mean")
+
+
+# ----------------------------------------------------------------------------- golden fixtures on the GPU
+
+def test_ieks_golden_gpu_fp64():
+    import os
+    gold_dir = os.path.join(os.path.dirname(__file__), "golden")
+    ys = np.load(os.path.join(gold_dir, "bearings_ys.npy")).astype(float)
+    gold = np.load(os.path.join(gold_dir, "ieks.npz"))
+    (ot, oo), (gt, go) = bearings_pair(0.01, 0.1, 0.5)
+    x0 = S.MVNSqrt(torch.tensor([-1.0, -1.0, 0.0, 0.0, 0.0], dtype=torch.float64), torch.eye(5, dtype=torch.float64))
+    res = S.iterated_smoothing(torch.as_tensor(ys), x0, gt, go, S.linearization.extended, None,
+                               criterion=lambda i, *_: i < 100)
+    np.testing.assert_array_almost_equal(np_(res.mean[1:]), gold["mean"], decimal=3)
+    np.testing.assert_array_almost_equal(cov(res.chol[1:]), gold["cov"], decimal=3)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_robustness_loglikelihood_gpu(dtype):
+    """The reference's FP32 GPU log-likelihoods of 20-iteration extended smoothers, as one ragged batch."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "robustness_small.npz"))
+    (ot, oo), (gt, go) = bearings_pair(0.01, 0.1, 0.5)
+    runs = d["ys"].shape[0]
+    x0 = S.MVNSqrt(torch.tensor([-4.0, -1.0, 2.0, 7.0, 3.0], dtype=torch.float64), torch.eye(5, dtype=torch.float64))
+    for ti, T in enumerate(d["Ts"]):
+        T = int(T)
+        ys = torch.as_tensor(d["ys"][:, :T], dtype=dtype)
+        nom = S.MVNSqrt(torch.tensor([-1.0, -1.0, 6.0, 4.0, 2.0], dtype=dtype).expand(runs, T + 1, 5),
+                        torch.eye(5, dtype=dtype).expand(runs, T + 1, 5, 5))
+        _, ell = S.iterated_smoothing(ys, x0, gt, go, S.linearization.extended, nom,
+                                      criterion=lambda i, *_: i < 20, return_loglikelihood=True)
+        g = d["ell_extended"][ti]
+        rel = np.abs(np_(ell) - g) / np.abs(g)
+        assert np.mean(rel < 1e-4) >= 0.8, (T, rel)

@@ -1,0 +1,135 @@
+"""Host-side checks that need no GPU: the C ABI loads and exports every symbol
+declared in include/*.h, struct layouts agree, argument validation maps to
+the reference's exception types, and the batch/criterion host logic."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+import sqrt_parallel_smoothers_gb300 as S
+from sqrt_parallel_smoothers_gb300 import _lib, methods
+from sqrt_parallel_smoothers_gb300.linearization import cubature, unscented, gauss_hermite, resolve
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(ss_\w+)\s*\(", src, flags=re.M))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    declared = _declared_symbols()
+    assert declared, "no declarations found"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert lib.ss_version() >= 10000
+
+
+def test_struct_layout():
+    assert ctypes.sizeof(_lib.SSModel) == 64
+    assert ctypes.sizeof(_lib.SSProblem) == 224
+
+
+def _problem(**kw):
+    p = _lib.SSProblem()
+    p.dtype, p.nx, p.ny, p.lin_method, p.batch = _lib.SS_F32, 5, 2, _lib.SS_LIN_CUBATURE, 1
+    p.gh_order = 3
+    dummy = ctypes.c_double(0)
+    for m in (p.transition, p.observation):
+        m.kind = _lib.SS_MODEL_LINEAR
+        m.matrix = m.noise_mean = m.noise_chol = ctypes.addressof(dummy)
+    p.offsets = ctypes.addressof(dummy)
+    p.total_steps = p.max_len = 10
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p, dummy
+
+
+def test_workspace_query_and_validation():
+    lib = _lib.load()
+    p, keep = _problem()
+    n = ctypes.c_size_t(0)
+    assert lib.ss_workspace_bytes(ctypes.byref(p), ctypes.byref(n)) == 0
+    assert n.value > 0
+    p2, keep2 = _problem(nx=40)
+    assert lib.ss_workspace_bytes(ctypes.byref(p2), ctypes.byref(n)) == _lib.SS_ERR_UNSUPPORTED
+    p3, keep3 = _problem(dtype=7)
+    assert lib.ss_workspace_bytes(ctypes.byref(p3), ctypes.byref(n)) == _lib.SS_ERR_INVALID
+    with pytest.raises(NotImplementedError):
+        _lib.check(_lib.SS_ERR_UNSUPPORTED)
+    with pytest.raises(ValueError):
+        _lib.check(_lib.SS_ERR_INVALID)
+    # a bearings observation needs ny = 2: (nx=5, ny=3) with bearings is not built
+    p4, keep4 = _problem(ny=3)
+    p4.observation.kind = _lib.SS_MODEL_BEARINGS
+    assert lib.ss_supported(ctypes.byref(p4)) == 0
+    p4.observation.kind = _lib.SS_MODEL_LINEAR
+    assert lib.ss_supported(ctypes.byref(p4)) == 1
+
+
+def test_calls_without_workspace_fail_cleanly():
+    lib = _lib.load()
+    p, keep = _problem()
+    buf = ctypes.c_double(0)
+    a = ctypes.addressof(buf)
+    # workspace too small: rejected on the host before any launch
+    rc = lib.ss_filter(ctypes.byref(p), a, a, a, 0, None, None, a, a, None, a, 8, None)
+    assert rc == _lib.SS_ERR_WORKSPACE
+
+
+def test_criterion_schedule():
+    assert methods._criterion_schedule(lambda i, *_: i < 10) == (10, 0.0)
+    assert methods._criterion_schedule(lambda i, *_: i < 1) == (1, 0.0)
+    assert methods._criterion_schedule(methods._default_criterion) == (100, 1e-6)
+    assert methods._criterion_schedule(S.MeanSquaredChange(1e-8, 7)) == (7, 1e-8)
+    with pytest.raises(NotImplementedError):
+        methods._criterion_schedule(lambda i, a, b: float(np.mean(a.mean)) > 0)
+
+
+def test_method_resolution():
+    import functools
+    assert resolve(cubature).code == _lib.SS_LIN_CUBATURE
+    m = resolve(functools.partial(unscented, alpha=0.5))
+    assert m.params["alpha"] == 0.5 and m.code == _lib.SS_LIN_UNSCENTED
+    assert resolve(functools.partial(gauss_hermite, order=5)).params["order"] == 5
+    with pytest.raises(NotImplementedError):
+        resolve(lambda model, x: None)
+
+
+def test_ragged_layout_roundtrip():
+    lengths = np.array([3, 0, 5, 1])
+    ys = torch.arange(4 * 5 * 2, dtype=torch.float32).reshape(4, 5, 2)
+    lay = methods._Layout(ys, lengths, None, None, torch.device("cpu"))
+    assert (lay.B, lay.N, lay.max_len) == (4, 9, 5)
+    assert lay.offsets.tolist() == [0, 3, 3, 8, 9]
+    np.testing.assert_array_equal(lay.ys[3:8].numpy(), ys[2, :5].numpy())
+    traj = torch.randn(4, 6, 3)
+    packed = lay.pack_states(traj, (3,))
+    assert packed.shape == (9 + 4, 3)
+    back = lay.unpack_states(packed, (3,))
+    for i, T in enumerate(lengths):
+        np.testing.assert_array_equal(back[i, :T + 1].numpy(), traj[i, :T + 1].numpy())
+
+
+def test_non_device_models_are_rejected():
+    with pytest.raises(NotImplementedError):
+        S.models.as_device_model(lambda x: x)
+
+
+def test_gh_roots_match_numpy():
+    # the library computes Gauss-Hermite roots by bisection; check against numpy's
+    from numpy.polynomial.hermite import hermgauss
+    for p in range(1, 9):
+        r, w = hermgauss(p)
+        from oracle.linearization import gauss_hermite_weights
+        wm, _, xi = gauss_hermite_weights(1, p)
+        np.testing.assert_allclose(np.sort(xi[:, 0]), np.sqrt(2) * np.sort(r), atol=1e-10)
