@@ -1,0 +1,398 @@
+"""Benchmark: smoother timesteps/s on one GB300, FP32 batched vs FP64 plain.
+
+Workload (the batched configuration): B = 1024 independent bearings-only
+sequences (coordinated-turn state, two bearings sensors, dt = 0.01), lengths
+drawn log-uniform in [50, 5000] (seed 0), sequence i simulated from seed i
+(+ 1024 * rank), iterated square-root cubature smoother, 10 filter-smoother
+calls from the prior mean broadcast over all steps, FP32.  One step = the
+whole 10-call smoother over the batch, replayed from one CUDA graph.
+``value`` = sum_i T_i / device time of a step (inputs resident).  The FP64
+plain path (B = 1, T = 5000, FP64, same method) is timed beside it.
+
+``--impl reference`` times the reference algorithm on the host CPU (the
+FP64 NumPy port in ``oracle/``: the reference's JAX code cannot be
+installed here) on a bounded sample of the same workload, with one process
+per host core.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+for _v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+    os.environ.setdefault(_v, "1")
+
+import numpy as np  # noqa: E402
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "smoother timesteps/s on 1 GB300: FP32 batched vs FP64 plain at fixed RMSE"
+UNIT = "timesteps/s"
+B_DEFAULT = 1024
+N_ITER = 10
+S1, S2 = (-1.5, 0.5), (1.0, 1.0)
+DT, QC, QW, SIGMA = 0.01, 0.1, 0.5, 0.05
+FP64_PLAIN_T = 5000
+
+
+def workload_config(B, lengths, C, G):
+    return {"workload": f"bearings-only coordinated-turn, iterated sqrt cubature smoother, B={B} ragged "
+                        f"T~logU[50,5000], {N_ITER} filter-smoother calls, FP32, one CUDA graph",
+            "batch": int(B), "sum_T": int(np.sum(lengths)), "max_T": int(np.max(lengths)),
+            "iterations": N_ITER, "nx": 5, "ny": 2, "linearization": "cubature", "chunk": C, "group": G,
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": "batch of sequences"}
+
+
+# ----------------------------------------------------------------------------- reference arm
+
+def _oracle_task(args):
+    ys, m0 = args
+    import oracle as O
+    Q, R = O.models.bearings_noise(QC, QW, SIGMA, DT)
+    tm = O.FunctionalModel(O.models.CoordinatedTurn(DT), O.MVNSqrt(np.zeros(5), np.linalg.cholesky(Q)))
+    om = O.FunctionalModel(O.models.Bearings(S1, S2), O.MVNSqrt(np.zeros(2), np.linalg.cholesky(R)))
+    T = ys.shape[0]
+    nom = O.MVNSqrt(np.repeat(m0[None], T + 1, 0), np.repeat(np.eye(5)[None], T + 1, 0))
+    res = O.methods.iterated_smoothing(ys.astype(np.float64), O.MVNSqrt(m0, np.eye(5)), tm, om,
+                                       O.linearization.cubature, nom, True, criterion=lambda i, *_: i < N_ITER)
+    return float(np.sum(res.mean))
+
+
+def cpu_sample(lengths, batch, budget_steps):
+    """The first sequences of the batch whose lengths sum to about ``budget_steps``."""
+    idx, tot = [], 0
+    for i, T in enumerate(lengths):
+        if tot >= budget_steps:
+            break
+        idx.append(i)
+        tot += int(T)
+    off = batch["offsets"]
+    return [batch["ys"][off[i]:off[i + 1]] for i in idx], tot
+
+
+def run_cpu(seqs, processes):
+    from sqrt_parallel_smoothers_gb300.data import BEARINGS_M0
+    tasks = [(y, BEARINGS_M0.copy()) for y in seqs]
+    t0 = time.perf_counter()
+    if processes <= 1:
+        for t in tasks:
+            _oracle_task(t)
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(processes) as pool:
+            pool.map(_oracle_task, tasks, chunksize=1)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from sqrt_parallel_smoothers_gb300 import data
+    lengths = data.ragged_lengths(B_DEFAULT, seed=0)
+    cores = os.cpu_count() or 1
+    sub = lengths[:max(cores * 2, 8)]
+    batch = data.bearings_batch(sub, qc=QC, qw=QW, sigma=SIGMA, dt=DT)
+    seqs, tot = cpu_sample(sub, batch, budget_steps=1500 * cores)
+    import multiprocessing as mp
+    times = []
+    with mp.get_context("spawn").Pool(cores) as pool:
+        from sqrt_parallel_smoothers_gb300.data import BEARINGS_M0
+        tasks = [(y, BEARINGS_M0.copy()) for y in seqs]
+        for k in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_oracle_task, tasks, chunksize=1)
+            if k >= args.warmup:
+                times.append(time.perf_counter() - t0)
+    t = float(np.mean(times))
+    value = tot / t
+    sample = f"{len(seqs)} sequences (sum T = {tot}) of the B=1024 batch, {N_ITER} calls, one process per core"
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(B_DEFAULT, lengths, 0, 0),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference JAX 0.4.30 is not installable offline; its algorithm is timed as the FP64 "
+                    "NumPy port in oracle/"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------- GPU arm
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def models(torch, S, dtype):
+    Q, R = S.data.bearings_noise(QC, QW, SIGMA, DT)
+    cQ = torch.as_tensor(np.linalg.cholesky(Q), dtype=dtype)
+    cR = torch.as_tensor(np.linalg.cholesky(R), dtype=dtype)
+    tm = S.FunctionalModel(S.models.CoordinatedTurn(DT), S.MVNSqrt(torch.zeros(5, dtype=dtype), cQ))
+    om = S.FunctionalModel(S.models.Bearings(S1, S2), S.MVNSqrt(torch.zeros(2, dtype=dtype), cR))
+    return tm, om
+
+
+def make_plan(torch, S, ys, offsets, dtype, chunk=0, group=0, graph=True, profile=False):
+    tm, om = models(torch, S, dtype)
+    m0 = torch.as_tensor(S.data.BEARINGS_M0, dtype=dtype)
+    x0 = S.MVNSqrt(m0, torch.eye(5, dtype=dtype))
+    n_states = int(ys.shape[0]) + len(offsets) - 1
+    nom = S.MVNSqrt(m0.expand(n_states, 5).contiguous(), torch.eye(5, dtype=dtype).expand(n_states, 5, 5).contiguous())
+    return S.IteratedSmootherPlan(torch.as_tensor(ys, dtype=dtype), x0, tm, om, S.linearization.cubature, nom,
+                                  criterion=S.FixedIterations(N_ITER), offsets=offsets, chunk=chunk, group=group,
+                                  graph=graph, profile=profile)
+
+
+def time_plan(torch, plan, steps, warmup, flush=None, sampler=None):
+    for _ in range(warmup):
+        plan.run()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    if sampler is not None:
+        sampler.start()
+    for k in range(steps):
+        if flush is not None:
+            flush.add_(1)
+        ev[k][0].record()
+        plan.run()
+        ev[k][1].record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler is not None else None
+    return [a.elapsed_time(b) for a, b in ev], clocks
+
+
+def position_rmse(mean, xs, offsets):
+    """Per-sequence RMSE of smoothed (x, y) positions against the simulated truth."""
+    out = []
+    for i in range(len(offsets) - 1):
+        a, b = offsets[i] + i, offsets[i + 1] + i + 1
+        d = mean[a + 1:b, :2] - xs[a + 1:b, :2]
+        out.append(float(np.sqrt(np.mean(np.sum(d * d, axis=1)))))
+    return np.array(out)
+
+
+# per-step algorithmic bytes (FP32, nx=5, ny=2) of each kernel: the compulsory
+# reads and writes of its inputs and outputs in minimal form (lower-triangular
+# factors counted by their 15 entries); see the design notes for the derivation.
+ALG_BYTES_PER_STEP = {
+    "lin": 4 * (20 + 60),            # nominal state in, F/cQ/bq/H/cR/c out
+    "filter_leaf": 4 * (60 + 2),     # linearised model + observation in
+    "filter_walk": 4 * (60 + 2 + 45),  # ... in, smoothing element out
+    "smoother_walk": 4 * (45 + 20),  # smoothing element in, smoothed state out
+}
+
+
+def gpu_arm(args):
+    import torch
+    import sqrt_parallel_smoothers_gb300 as S
+    from sqrt_parallel_smoothers_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    lengths = S.data.ragged_lengths(args.batch, seed=0)
+    batch = S.data.bearings_batch(lengths, qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=rank * args.batch)
+    offsets = batch["offsets"]
+    plan = make_plan(torch, S, batch["ys"], offsets, torch.float32, args.chunk, args.group)
+    C = args.chunk or 16
+    G = args.group or 8
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+    sampler = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    step_ms, clocks = time_plan(torch, plan, args.steps, args.warmup, flush, sampler)
+    torch.cuda.synchronize()
+    barrier()
+    ms = float(np.mean(step_ms))
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    sum_T = int(lengths.sum())
+    value = world * sum_T / (ms * 1e-3)
+    launches = plan.launches_per_run * args.steps
+
+    # e2e: host observations in (pinned), the smoothed trajectory out (pinned), every step
+    ys_host = torch.as_tensor(batch["ys"], dtype=torch.float32).pin_memory()
+    m_host = torch.empty(plan.mean.shape, dtype=torch.float32).pin_memory()
+    L_host = torch.empty(plan.chol.shape, dtype=torch.float32).pin_memory()
+    for _ in range(args.warmup):
+        plan.run_host(ys_host, m_host, L_host)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        plan.run_host(ys_host, m_host, L_host)
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e = {"value": world * sum_T / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(ys_host.nbytes),
+           "d2h_bytes_per_step": int(m_host.nbytes + L_host.nbytes), "ms_per_step": e2e_ms,
+           "path": "IteratedSmootherPlan.run_host: pinned host copy-in, graph replay, copy-out"}
+    mean32 = m_host.numpy().astype(np.float64)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simulator of the reference's "
+                                                       "bearings experiment)",
+            "config": workload_config(args.batch, lengths, C, G), "e2e": e2e, "gpu_launches": int(launches),
+            "clocks": clocks}
+
+    if args.only_main:
+        print(json.dumps(line), flush=True)
+        return 0
+
+    # per-kernel device times from CUDA events captured in a second graph (roofline)
+    pplan = make_plan(torch, S, batch["ys"], offsets, torch.float32, args.chunk, args.group, profile=True)
+    totals = {}
+    for _ in range(args.steps):
+        flush.add_(1)
+        pplan.run()
+        torch.cuda.synchronize()
+        for k, (n, t) in _lib.profile_read().items():
+            a = totals.setdefault(k, [0, 0.0])
+            a[0] += n
+            a[1] += t
+    del pplan
+    torch.cuda.synchronize()
+    _lib.profile_reset()
+    kern = {k: {"launches": v[0], "total_ms": v[1], "avg_ms": v[1] / max(v[0], 1)} for k, v in totals.items()}
+    tot = sum(v["total_ms"] for v in kern.values()) or 1.0
+    for v in kern.values():
+        v["share"] = v["total_ms"] / tot
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    alg = ALG_BYTES_PER_STEP.get(dom)
+    if alg is not None:
+        achieved = alg * sum_T / (kern[dom]["avg_ms"] * 1e-3) / 1e9
+        line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                            "frac": achieved / hbm_peak, "traffic": None,
+                            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                            "alg_bytes_per_launch": alg * sum_T}
+    line["kernels"] = kern
+
+    # FP64 plain: one sequence, T = 5000, FP64
+    one = S.data.bearings_batch(np.array([FP64_PLAIN_T]), qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=10_000)
+    plan64 = make_plan(torch, S, one["ys"], one["offsets"], torch.float64)
+    ms64, _ = time_plan(torch, plan64, max(3, min(args.steps, 5)), 1, flush)
+    v64 = FP64_PLAIN_T / (float(np.mean(ms64)) * 1e-3)
+    line["fp64_plain"] = {"value": v64, "unit": UNIT, "T": FP64_PLAIN_T, "ms_per_step": float(np.mean(ms64))}
+    line["ratio_vs_fp64_plain"] = value / world / v64
+
+    # accuracy: FP32 batched vs FP64 batched (same GPU path, FP64) against the simulated truth
+    plan_acc = make_plan(torch, S, batch["ys"], offsets, torch.float64, graph=False)
+    plan_acc.run()
+    torch.cuda.synchronize()
+    mean64 = plan_acc.mean.cpu().numpy()
+    del plan_acc
+    r32 = position_rmse(mean32, batch["xs"].astype(np.float64), offsets)
+    r64 = position_rmse(mean64, batch["xs"].astype(np.float64), offsets)
+    rel = np.abs(r32 - r64) / np.maximum(r64, 1e-12)
+    line["accuracy"] = {"rmse_fp32_median": float(np.median(r32)), "rmse_fp64_median": float(np.median(r64)),
+                        "rmse_rel_diff_median": float(np.median(rel)), "rmse_rel_diff_p95": float(np.quantile(rel, 0.95)),
+                        "frac_within_1pct": float(np.mean(rel <= 0.01)),
+                        "max_abs_mean_diff_fp32_vs_fp64": float(np.max(np.abs(mean32 - mean64)))}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        seqs, tot = cpu_sample(lengths, batch, budget_steps=6000)
+        t_cpu = run_cpu(seqs, 1)
+        line["cpu_baseline"] = {"value": tot / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"first {len(seqs)} sequences of the batch (sum T = {tot}), "
+                                          f"{N_ITER} calls, FP64 NumPy port, 1 process"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--batch", type=int, default=B_DEFAULT)
+    ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--group", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-main", action="store_true", help="time the FP32 batched smoother only")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

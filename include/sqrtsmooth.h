@@ -147,6 +147,18 @@ int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void*
                 int32_t* out_iters, uint32_t* out_flags, void* workspace, size_t workspace_bytes,
                 ss_stream_t stream);
 
+/* Instrumentation (no counterpart in the reference, which has no tracing):
+ * a counter of kernels launched by this library, and per-kernel CUDA-event
+ * timing.  While profiling is enabled every launch is bracketed by two events
+ * on its stream (also when the launches are captured into a CUDA graph: the
+ * events are then re-recorded by every replay).  ss_profile_read waits for the
+ * recorded events and writes {"kernel": [launches, total_ms], ...} as JSON;
+ * ss_profile_reset destroys them (after any graph holding them is gone). */
+long long ss_launch_count(void);
+int ss_profile_enable(int on);
+int ss_profile_read(char* buf, size_t len);
+int ss_profile_reset(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -220,6 +220,9 @@ def filtering(observations, x0, transition_model, observation_model, linearizati
     else:
         nominal_trajectory = _default_nominal(type(x0), T + 1, nx)
     sqrt = isinstance(x0, MVNSqrt)
+    if T == 0:  # an empty sequence: the trajectory is the prior alone
+        res = type(x0)(m0[None], c0[None])
+        return (res, 0.0) if return_loglikelihood else res
     n_prev = type(x0)(*(np.asarray(v, dtype=float)[:-1] for v in nominal_trajectory))
     n_next = type(x0)(*(np.asarray(v, dtype=float)[1:] for v in nominal_trajectory))
     F, Q_, b = linearization_method(transition_model, n_prev)
@@ -273,6 +276,8 @@ def smoothing(transition_model, filter_trajectory, linearization_method, nominal
     else:
         nominal_trajectory = _default_nominal(type(filter_trajectory), Tp1, nx)
     sqrt = isinstance(filter_trajectory, MVNSqrt)
+    if Tp1 == 1:
+        return type(filter_trajectory)(fm, fc)
     nom = type(filter_trajectory)(*(np.asarray(v, dtype=float)[:-1] for v in nominal_trajectory))
     F, Q_, b = linearization_method(transition_model, nom)
     if sqrt:

@@ -10,9 +10,10 @@ __version__ = "1.0.0"
 
 from ._base import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsModel
 from .methods import (filtering, smoothing, filter_smoother, iterated_smoothing, linearize, FixedIterations,
-                      MeanSquaredChange)
+                      MeanSquaredChange, IteratedSmootherPlan)
 from . import linearization, models, data
 
 __all__ = ["MVNSqrt", "MVNStandard", "FunctionalModel", "ConditionalMomentsModel", "filtering", "smoothing",
            "filter_smoother", "iterated_smoothing", "linearize", "FixedIterations", "MeanSquaredChange",
+           "IteratedSmootherPlan",
            "linearization", "models", "data"]

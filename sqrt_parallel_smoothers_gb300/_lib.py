@@ -16,7 +16,8 @@ SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS = 0, 1, 2
 SS_MAX_GH_ORDER = 8
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
-            "ss_filter", "ss_smooth", "ss_iterated")
+            "ss_filter", "ss_smooth", "ss_iterated", "ss_launch_count", "ss_profile_enable", "ss_profile_read",
+            "ss_profile_reset")
 
 
 class SSModel(ctypes.Structure):
@@ -64,8 +65,12 @@ def load():
         lib.ss_smooth.argtypes = [PP, P, P, P, P, P, P, P, ctypes.c_size_t, P]
         lib.ss_iterated.argtypes = [PP, P, P, P, ctypes.c_int32, P, P, ctypes.c_int32, ctypes.c_double,
                                     P, P, P, P, P, P, ctypes.c_size_t, P]
+        lib.ss_profile_enable.argtypes = [ctypes.c_int]
+        lib.ss_profile_read.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         for name in EXPORTED:
-            getattr(lib, name).restype = ctypes.c_int if name != "ss_status_string" else ctypes.c_char_p
+            getattr(lib, name).restype = ctypes.c_int
+        lib.ss_status_string.restype = ctypes.c_char_p
+        lib.ss_launch_count.restype = ctypes.c_longlong
         _handle = lib
         return lib
 
@@ -84,3 +89,24 @@ def check(status):
     if status == SS_ERR_UNSUPPORTED:
         raise NotImplementedError(msg)
     raise SqrtSmoothError(msg)
+
+
+def launch_count():
+    """Kernels launched by the library in this process so far."""
+    return int(load().ss_launch_count())
+
+
+def profile_enable(on=True):
+    load().ss_profile_enable(1 if on else 0)
+
+
+def profile_read():
+    """``{kernel: (launches, total_ms)}`` over the events recorded while profiling."""
+    import json
+    buf = ctypes.create_string_buffer(1 << 16)
+    check(load().ss_profile_read(buf, len(buf)))
+    return {k: (int(v[0]), float(v[1])) for k, v in json.loads(buf.value.decode()).items()}
+
+
+def profile_reset():
+    load().ss_profile_reset()

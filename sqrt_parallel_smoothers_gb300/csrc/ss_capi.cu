@@ -1,7 +1,13 @@
 // C ABI of the library: argument validation and dispatch to the compiled
 // (dtype, nx, ny) instantiations.
+#include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
 
 #include "ss_dims.h"
 #include "ss_run.cuh"
@@ -108,6 +114,24 @@ int fill_rule(const ss_problem& p, RuleArgs& r) {
   return SS_OK;
 }
 
+// ----------------------------------------------------------------------------- instrumentation
+
+static std::atomic<long long> g_launches{0};
+static std::atomic<bool> g_profiling{false};
+static std::mutex g_prof_mu;
+struct ProfRec {
+  const char* name;
+  cudaEvent_t start, stop;
+};
+static std::vector<ProfRec> g_prof;
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+bool profiling_on() { return g_profiling.load(std::memory_order_relaxed); }
+void profile_push(const char* name, cudaEvent_t start, cudaEvent_t stop) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  g_prof.push_back({name, start, stop});
+}
+
 static int validate(const ss_problem* p) {
   if (p == nullptr) return SS_ERR_INVALID;
   if (p->dtype != SS_F32 && p->dtype != SS_F64) return SS_ERR_INVALID;
@@ -141,6 +165,52 @@ using namespace ss;
 extern "C" {
 
 int ss_version(void) { return 10000; }
+
+long long ss_launch_count(void) { return g_launches.load(); }
+
+int ss_profile_enable(int on) {
+  g_profiling.store(on != 0);
+  return SS_OK;
+}
+
+int ss_profile_reset(void) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  for (const ProfRec& r : g_prof) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  g_prof.clear();
+  return SS_OK;
+}
+
+int ss_profile_read(char* buf, size_t len) {
+  if (buf == nullptr || len == 0) return SS_ERR_INVALID;
+  std::map<std::string, std::pair<long long, double>> acc;
+  {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (const ProfRec& r : g_prof) {
+      if (cudaEventSynchronize(r.stop) != cudaSuccess) return SS_ERR_CUDA;
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, r.start, r.stop) != cudaSuccess) return SS_ERR_CUDA;
+      auto& a = acc[r.name];
+      a.first += 1;
+      a.second += ms;
+    }
+  }
+  std::string out = "{";
+  bool first = true;
+  for (const auto& kv : acc) {
+    char item[160];
+    std::snprintf(item, sizeof(item), "%s\"%s\": [%lld, %.6f]", first ? "" : ", ", kv.first.c_str(),
+                  kv.second.first, kv.second.second);
+    out += item;
+    first = false;
+  }
+  out += "}";
+  if (out.size() + 1 > len) return SS_ERR_INVALID;
+  std::memcpy(buf, out.c_str(), out.size() + 1);
+  return SS_OK;
+}
 
 const char* ss_status_string(int status) {
   switch (status) {

@@ -117,9 +117,30 @@ inline int slr_form_of(const ss_problem& p, bool fp32) {
   return fp32 ? SS_SLR_RESIDUAL : SS_SLR_DOWNDATE;
 }
 
-#define SS_CHECK_LAUNCH()                         \
-  do {                                            \
-    if (cudaGetLastError() != cudaSuccess) return SS_ERR_CUDA; \
+// Instrumentation (ss_capi.cu): a launch counter and optional per-kernel
+// CUDA-event timing.  Events are recorded on the launching stream around each
+// kernel, so they also time kernels replayed from a captured CUDA graph.
+void count_launch();
+bool profiling_on();
+void profile_push(const char* name, cudaEvent_t start, cudaEvent_t stop);
+
+#define SS_LAUNCH(NAME, ST, ...)                                           \
+  do {                                                                     \
+    cudaEvent_t ss_e0_ = nullptr;                                          \
+    const bool ss_prof_ = ss::profiling_on();                              \
+    if (ss_prof_) {                                                        \
+      cudaEventCreate(&ss_e0_);                                            \
+      cudaEventRecord(ss_e0_, ST);                                         \
+    }                                                                      \
+    __VA_ARGS__;                                                           \
+    if (cudaGetLastError() != cudaSuccess) return SS_ERR_CUDA;             \
+    ss::count_launch();                                                    \
+    if (ss_prof_) {                                                        \
+      cudaEvent_t ss_e1_ = nullptr;                                        \
+      cudaEventCreate(&ss_e1_);                                            \
+      cudaEventRecord(ss_e1_, ST);                                         \
+      ss::profile_push(NAME, ss_e0_, ss_e1_);                              \
+    }                                                                      \
   } while (0)
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block > 0 ? (n + block - 1) / block : 1); }
@@ -129,13 +150,12 @@ template <typename R, int NX, int NY, class TF, class OF>
 inline int launch_lin_method(const LinArgs<R>& a, int method, cudaStream_t st) {
   const unsigned grid = grid_for(a.total, 128);
   switch (method) {
-    case SS_LIN_EXTENDED: lin_kernel<R, NX, NY, TF, OF, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_CUBATURE: lin_kernel<R, NX, NY, TF, OF, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_UNSCENTED: lin_kernel<R, NX, NY, TF, OF, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_GAUSS_HERMITE: lin_kernel<R, NX, NY, TF, OF, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_EXTENDED: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_CUBATURE: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_UNSCENTED: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_GAUSS_HERMITE: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a)); break;
     default: return SS_ERR_UNSUPPORTED;
   }
-  SS_CHECK_LAUNCH();
   return SS_OK;
 }
 
@@ -175,13 +195,12 @@ template <typename R, int DIN, int DOUT, class Fn>
 inline int launch_points_method(const PointArgs<R>& a, int method, cudaStream_t st) {
   const unsigned grid = grid_for(a.n, 128);
   switch (method) {
-    case SS_LIN_EXTENDED: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_CUBATURE: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_UNSCENTED: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a); break;
-    case SS_LIN_GAUSS_HERMITE: lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a); break;
+    case SS_LIN_EXTENDED: SS_LAUNCH("lin_points", st, lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_CUBATURE: SS_LAUNCH("lin_points", st, lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_UNSCENTED: SS_LAUNCH("lin_points", st, lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a)); break;
+    case SS_LIN_GAUSS_HERMITE: SS_LAUNCH("lin_points", st, lin_points_kernel<R, DIN, DOUT, Fn, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a)); break;
     default: return SS_ERR_UNSUPPORTED;
   }
-  SS_CHECK_LAUNCH();
   return SS_OK;
 }
 
@@ -215,8 +234,7 @@ struct Runner {
     geo.L = y.L;
     for (int l = 0; l <= MAX_LEVELS; ++l) geo.lvl[l] = nullptr;
     for (int l = 1; l <= y.L; ++l) geo.lvl[l] = at<int64_t>(y.lvl) + (size_t)(l - 1) * y.lvl_stride;
-    plan_kernel<512><<<1, 512, 0, st>>>(geo, at<int64_t>(y.lvl), (int64_t)y.lvl_stride);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("plan", st, plan_kernel<512><<<1, 512, 0, st>>>(geo, at<int64_t>(y.lvl), (int64_t)y.lvl_stride));
     std::memset(&sa, 0, sizeof(sa));
     sa.g = geo;
     sa.ys = static_cast<const R*>(c.ys);
@@ -261,42 +279,33 @@ struct Runner {
   // Filter scan: level-1 summaries must already be in fsum[1] (filter_leaf).
   int filter_scan() {
     for (int l = 1; l < y.L; ++l) {
-      filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("filter_up", st, filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
     }
-    filter_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("filter_top", st, filter_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("filter_down", st, filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
     }
     return SS_OK;
   }
 
   int filter_pass(bool emit_smoother) {
-    filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("filter_leaf", st, filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     int rc = filter_scan();
     if (rc) return rc;
     sa.emit_smoother = emit_smoother ? 1 : 0;
-    filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("filter_walk", st, filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     return SS_OK;
   }
 
   int smoother_scan_and_walk() {
     for (int l = 1; l < y.L; ++l) {
-      smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("smoother_up", st, smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
     }
-    smoother_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("smoother_top", st, smoother_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("smoother_down", st, smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
     }
-    smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("smoother_walk", st, smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     return SS_OK;
   }
 
@@ -311,8 +320,7 @@ struct Runner {
     rc = filter_pass(false);
     if (rc) return rc;
     if (c.out_ell) {
-      ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, nullptr);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, nullptr));
     }
     return SS_OK;
   }
@@ -326,8 +334,7 @@ struct Runner {
     sa.in_L = static_cast<const R*>(c.in_L);
     sa.out_m = static_cast<R*>(c.out_m);
     sa.out_L = static_cast<R*>(c.out_L);
-    smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("smoother_leaf", st, smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     return smoother_scan_and_walk();
   }
 
@@ -339,8 +346,7 @@ struct Runner {
     int32_t* iters = at<int32_t>(y.iters);
     double* mse = at<double>(y.mse);
     const bool has_init = c.nom_m != nullptr;
-    init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, c.out_flags, 0);
-    SS_CHECK_LAUNCH();
+    SS_LAUNCH("init_iter", st, init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, c.out_flags, 0));
     const int calls = c.n_iter > 1 ? c.n_iter : 1;
     R* bufm[2] = {at<R>(y.nomA_m), at<R>(y.nomB_m)};
     R* bufL[2] = {at<R>(y.nomA_L), at<R>(y.nomB_L)};
@@ -372,8 +378,7 @@ struct Runner {
       rc = smoother_scan_and_walk();
       if (rc) return rc;
       if (tol_mode && counted) {
-        converge_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NX, c.tol, mse, active, iters);
-        SS_CHECK_LAUNCH();
+        SS_LAUNCH("converge", st, converge_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NX, c.tol, mse, active, iters));
       }
       cur_m = om;
       cur_L = oL;
@@ -388,17 +393,14 @@ struct Runner {
       sa.ll_chunk = at<double>(y.ll);
       rc = filter_pass(false);
       if (rc) return rc;
-      ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, c.out_flags);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, c.out_flags));
     }
     if (c.out_iters || (c.out_flags && tol_mode)) {
       if (!tol_mode) {
-        init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, nullptr, calls);
-        SS_CHECK_LAUNCH();
+        SS_LAUNCH("init_iter", st, init_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, mse, nullptr, calls));
       }
-      finish_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, c.out_iters, c.out_flags,
-                                                                 tol_mode ? 1 : 0);
-      SS_CHECK_LAUNCH();
+      SS_LAUNCH("finish_iter", st, finish_iter_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(p.batch, active, iters, c.out_iters, c.out_flags,
+                                                                 tol_mode ? 1 : 0));
     }
     return SS_OK;
   }

@@ -220,6 +220,9 @@ _WS = {}
 
 
 def _workspace(nbytes, device):
+    if torch.cuda.is_current_stream_capturing():
+        # a graph keeps its own workspace, allocated from the graph's private pool
+        return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
     key = (device.index, torch.cuda.current_stream(device).cuda_stream)
     buf = _WS.get(key)
     if buf is None or buf.numel() < nbytes:
@@ -557,3 +560,103 @@ def _dummy_transition(nx, dtype, device):
     fn = LinearModel(torch.eye(nx))
     return fn, _as(fn.A, dtype, device), torch.zeros(nx, dtype=dtype, device=device), \
         torch.eye(nx, dtype=dtype, device=device)
+
+
+# ----------------------------------------------------------------------------- graph-replayed plans
+
+class IteratedSmootherPlan:
+    """An iterated smoother staged once and replayed as a CUDA graph.
+
+    Arguments are those of :func:`iterated_smoothing`.  Construction packs
+    and uploads every input, runs the smoother once (workspace allocation,
+    warm-up) and captures the whole N-iteration loop - every kernel of every
+    iteration - into one CUDA graph.  :meth:`run` replays it on the current
+    stream; :meth:`set_observations` refreshes the observations in place (same
+    shapes) and :meth:`run_host` does copy-in, replay and copy-out from and to
+    host buffers.  Results live in :attr:`mean` / :attr:`chol` (packed
+    ``(sum (T_i+1), nx)`` layout) and :attr:`ell` (when requested).  With
+    ``profile=True`` every captured kernel is bracketed by CUDA events that
+    each replay re-records; ``_lib.profile_read()`` returns the last replay's
+    per-kernel times (call ``_lib.profile_reset()`` only after the plan is gone)."""
+
+    def __init__(self, observations, x0, transition_model, observation_model, linearization_method,
+                 init_nominal_trajectory=None, criterion=_default_criterion, return_loglikelihood=False, *,
+                 lengths=None, offsets=None, chunk=0, group=0, slr_form=0, graph=True, profile=False):
+        method = _check_common(x0, True, linearization_method)
+        if init_nominal_trajectory is not None:
+            are_inputs_compatible(x0, init_nominal_trajectory)
+        n_calls, tol = _criterion_schedule(criterion)
+        dev = _device()
+        lay = _Layout(observations, lengths, offsets, None, dev)
+        nx = int(torch.as_tensor(x0.mean).shape[-1])
+        fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+        fn_o, o_mat, o_qm, o_qL = _model_tensors(observation_model, nx, lay.ny, lay.dtype, dev)
+        m0, L0, per = _prior(x0, lay, nx)
+        im, iL = _nominal(init_nominal_trajectory, lay, nx)
+        icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, slr_form,
+                     [per, int(bool(return_loglikelihood)), n_calls])
+        fcfg = _fcfg(method, fn_t, fn_o, [tol])
+        self.layout, self.nx = lay, nx
+        self._args = (lay.ys, lay.offsets, m0, L0, im, iL, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg)
+        self.steps = lay.N
+        self.graph = None
+        stream = torch.cuda.Stream(dev)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(stream):
+            self._outs = _iterated_op(*self._args)      # warm-up, allocates the cached workspace
+            if graph:
+                n0 = _lib.launch_count()
+                self._outs = _iterated_op(*self._args)
+                self.launches_per_run = _lib.launch_count() - n0
+                g = torch.cuda.CUDAGraph()
+                if profile:
+                    # per-kernel CUDA events recorded by every replay (read with _lib.profile_read)
+                    _lib.profile_reset()
+                    _lib.profile_enable(True)
+                try:
+                    with torch.cuda.graph(g, stream=stream):
+                        self._outs = _iterated_op(*self._args)
+                finally:
+                    if profile:
+                        _lib.profile_enable(False)
+                self.graph = g
+        torch.cuda.current_stream(dev).wait_stream(stream)
+        torch.cuda.synchronize(dev)
+
+    @property
+    def mean(self):
+        return self._outs[0]
+
+    @property
+    def chol(self):
+        return self._outs[1]
+
+    @property
+    def ell(self):
+        return self._outs[2]
+
+    def run(self):
+        """Replay the captured loop (or run it directly when built with ``graph=False``)."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._outs = _iterated_op(*self._args)
+        return self._outs
+
+    def set_observations(self, ys_packed, non_blocking=True):
+        """Copy new packed observations ``(sum T_i, ny)`` into the staged buffer."""
+        self._args[0].copy_(ys_packed, non_blocking=non_blocking)
+
+    def run_host(self, ys_host, out_mean_host, out_chol_host=None):
+        """Host -> device copy of ``ys_host``, replay, device -> host copy of the results."""
+        self.set_observations(ys_host)
+        self.run()
+        out_mean_host.copy_(self.mean, non_blocking=True)
+        if out_chol_host is not None:
+            out_chol_host.copy_(self.chol, non_blocking=True)
+        return out_mean_host, out_chol_host
+
+    def result(self):
+        """The smoothed trajectory in the caller's layout."""
+        lay, nx = self.layout, self.nx
+        return MVNSqrt(lay.unpack_states(self.mean, (nx,)), lay.unpack_states(self.chol, (nx, nx)))

@@ -21,7 +21,7 @@ def _declared_symbols():
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         src = open(h).read()
-        names |= set(re.findall(r"^\s*(?:int|const char\*)\s+(ss_\w+)\s*\(", src, flags=re.M))
+        names |= set(re.findall(r"^\s*(?:int|const char\*|long long)\s+(ss_\w+)\s*\(", src, flags=re.M))
     return names
 
 
