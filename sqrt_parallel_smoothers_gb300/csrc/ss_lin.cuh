@@ -60,6 +60,132 @@ SS_DEV int num_points(const RuleArgs& ru) {
 // and avoids the cancellation of the downdate in FP32.
 enum { SS_SLR_DOWNDATE = 1, SS_SLR_RESIDUAL = 2 };
 
+// Symmetric rules (cubature, unscented) with the model evaluated once per
+// point.  Point k = 0 is the unscented centre; points (+j, -j) are
+// m +- sc C[:, j].  With f_j^+- = f(m +- sc C[:, j]):
+//   S[:, j] = w sc (f_j^+ - f_j^-)                       (so that F = S C^{-1})
+//   residual of both points of pair j:  (f_j^+ + f_j^-)/2 - m_f
+// so the residual form needs one column sqrt(2w) ((f^+ + f^-)/2 - m_f) per
+// pair (plus the centre's sqrt(wc0) (f_0 - m_f)), and the downdate form the
+// 2n(+1) columns sqrt(wc_k) (f_k - m_f).  Either matrix is triangularised by
+// one Householder tria.
+template <typename R, int DIN, int DOUT, class Fn, int METHOD>
+SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], const R (&qm)[DOUT],
+                                const R (&qc)[DOUT][DOUT], const RuleArgs& ru, int slr_form,
+                                R (&F)[DOUT][DIN], R (&L)[DOUT][DOUT], R (&b)[DOUT]) {
+  constexpr bool UT = (METHOD == SS_LIN_UNSCENTED);
+  constexpr int NC = UT ? 1 : 0;  // centre point
+  R sc, w, wm0 = R(0), wc0 = R(0);
+  if constexpr (UT) {
+    sc = rule_ut<R>(ru, 0);
+    wm0 = rule_ut<R>(ru, 1);
+    wc0 = rule_ut<R>(ru, 2);
+    w = rule_ut<R>(ru, 3);
+  } else {
+    sc = ss_sqrt(R(DIN));
+    w = R(1) / R(2 * DIN);
+  }
+  R fp[DIN][DOUT], fn[DIN][DOUT], f0[DOUT];
+  if constexpr (UT) f.eval(m, f0);
+  SS_UNROLL
+  for (int j = 0; j < DIN; ++j) {
+    R xp[DIN], xn[DIN];
+    SS_UNROLL
+    for (int i = 0; i < DIN; ++i) {
+      const R d = (i >= j) ? sc * C[i][j] : R(0);
+      xp[i] = m[i] + d;
+      xn[i] = m[i] - d;
+    }
+    f.eval(xp, fp[j]);
+    f.eval(xn, fn[j]);
+  }
+  R mf[DOUT];
+  SS_UNROLL
+  for (int i = 0; i < DOUT; ++i) {
+    R s = R(0);
+    SS_UNROLL
+    for (int j = 0; j < DIN; ++j) s += fp[j][i] + fn[j][i];
+    mf[i] = w * s;
+    if constexpr (UT) mf[i] += wm0 * f0[i];
+  }
+  R S[DOUT][DIN];
+  SS_UNROLL
+  for (int i = 0; i < DOUT; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < DIN; ++j) S[i][j] = w * sc * (fp[j][i] - fn[j][i]);
+  }
+  // F^T = C^{-T} S^T
+  {
+    R Ft[DIN][DOUT];
+    SS_UNROLL
+    for (int i = 0; i < DIN; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) Ft[i][j] = S[j][i];
+    }
+    solve_lower_T<R, DIN, DOUT>(C, Ft);
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DIN; ++j) F[i][j] = Ft[j][i];
+    }
+  }
+  if (slr_form == SS_SLR_RESIDUAL) {
+    constexpr int NCOL = NC + DIN + DOUT;
+    R M[DOUT][NCOL];
+    const R s2w = ss_sqrt(R(2) * w);
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      if constexpr (UT) M[i][0] = ss_sqrt(wc0) * (f0[i] - mf[i]);
+      SS_UNROLL
+      for (int j = 0; j < DIN; ++j) M[i][NC + j] = s2w * (R(0.5) * (fp[j][i] + fn[j][i]) - mf[i]);
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) M[i][NC + DIN + j] = qc[i][j];
+    }
+    tria<R, DOUT, NCOL>(M);
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) L[i][j] = (j <= i) ? M[i][j] : R(0);
+    }
+  } else {
+    constexpr int NCOL = NC + 2 * DIN + DOUT;
+    R M[DOUT][NCOL];
+    const R sw = ss_sqrt(w);
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      if constexpr (UT) M[i][0] = ss_sqrt(wc0) * (f0[i] - mf[i]);
+      SS_UNROLL
+      for (int j = 0; j < DIN; ++j) {
+        M[i][NC + j] = sw * (fp[j][i] - mf[i]);
+        M[i][NC + DIN + j] = sw * (fn[j][i] - mf[i]);
+      }
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) M[i][NC + 2 * DIN + j] = qc[i][j];
+    }
+    tria<R, DOUT, NCOL>(M);
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) L[i][j] = (j <= i) ? M[i][j] : R(0);
+    }
+    // downdate by the columns of F C (= S)
+    SS_UNROLL
+    for (int j = 0; j < DIN; ++j) {
+      R col[DOUT];
+      SS_UNROLL
+      for (int i = 0; i < DOUT; ++i) col[i] = S[i][j];
+      chol_update<R, DOUT>(L, col, R(-1));
+    }
+  }
+  SS_UNROLL
+  for (int i = 0; i < DOUT; ++i) {
+    R s = mf[i] + qm[i];
+    SS_UNROLL
+    for (int j = 0; j < DIN; ++j) s -= F[i][j] * m[j];
+    b[i] = s;
+  }
+}
+
 template <typename R, int DIN, int DOUT, class Fn, int METHOD>
 SS_DEV void linearize(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], const R (&qm)[DOUT],
                       const R (&qc)[DOUT][DOUT], const RuleArgs& ru, int slr_form,
@@ -78,7 +204,10 @@ SS_DEV void linearize(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], co
       SS_UNROLL
       for (int j = 0; j < DOUT; ++j) L[i][j] = qc[i][j];
     }
+  } else if constexpr (METHOD == SS_LIN_CUBATURE || METHOD == SS_LIN_UNSCENTED) {
+    linearize_symmetric<R, DIN, DOUT, Fn, METHOD>(f, m, C, qm, qc, ru, slr_form, F, L, b);
   } else {
+    // Gauss-Hermite: p^n points streamed (recomputed per pass) with Givens updates
     const int np = num_points<DIN, METHOD>(ru);
     // pass 1: m_f = sum_k wm_k f(m + C xi_k)
     R mf[DOUT];

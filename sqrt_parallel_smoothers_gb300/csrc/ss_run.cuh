@@ -124,13 +124,21 @@ void count_launch();
 bool profiling_on();
 void profile_push(const char* name, cudaEvent_t start, cudaEvent_t stop);
 
+// During stream capture an event record only becomes a graph node (re-recorded
+// by every replay) with cudaEventRecordExternal.
+inline void record_event(cudaEvent_t e, cudaStream_t st) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cs);
+  cudaEventRecordWithFlags(e, st, cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+}
+
 #define SS_LAUNCH(NAME, ST, ...)                                           \
   do {                                                                     \
     cudaEvent_t ss_e0_ = nullptr;                                          \
     const bool ss_prof_ = ss::profiling_on();                              \
     if (ss_prof_) {                                                        \
       cudaEventCreate(&ss_e0_);                                            \
-      cudaEventRecord(ss_e0_, ST);                                         \
+      ss::record_event(ss_e0_, ST);                                        \
     }                                                                      \
     __VA_ARGS__;                                                           \
     if (cudaGetLastError() != cudaSuccess) return SS_ERR_CUDA;             \
@@ -138,7 +146,7 @@ void profile_push(const char* name, cudaEvent_t start, cudaEvent_t stop);
     if (ss_prof_) {                                                        \
       cudaEvent_t ss_e1_ = nullptr;                                        \
       cudaEventCreate(&ss_e1_);                                            \
-      cudaEventRecord(ss_e1_, ST);                                         \
+      ss::record_event(ss_e1_, ST);                                        \
       ss::profile_push(NAME, ss_e0_, ss_e1_);                              \
     }                                                                      \
   } while (0)
