@@ -38,14 +38,18 @@ N_ITER = 10
 S1, S2 = (-1.5, 0.5), (1.0, 1.0)
 DT, QC, QW, SIGMA = 0.01, 0.1, 0.5, 0.05
 FP64_PLAIN_T = 5000
+# prior centred on the simulator's initial state (x, y, vx, vy) = (0.1, 0.2, 1, 0) with
+# the simulator's mean turn rate 1, P0 = I; the initial trajectory is this mean broadcast
+PRIOR_M0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
 
 
 def workload_config(B, lengths, C, G):
     return {"workload": f"bearings-only coordinated-turn, iterated sqrt cubature smoother, B={B} ragged "
-                        f"T~logU[50,5000], default start + {N_ITER} filter-smoother calls, FP32, one CUDA graph",
+                        f"T~logU[50,5000], {N_ITER} filter-smoother calls from the prior mean broadcast, FP32, "
+                        f"one CUDA graph",
             "batch": int(B), "sum_T": int(np.sum(lengths)), "max_T": int(np.max(lengths)),
-            "iterations": N_ITER, "passes": N_ITER + 1, "init": "reference default (pass at zero nominal)",
-            "prior": "m0=(-4,-1,2,7,3), P0=I", "nx": 5, "ny": 2, "linearization": "cubature", "chunk": C, "group": G,
+            "iterations": N_ITER, "init": "prior mean broadcast", "prior": "m0=(0.1,0.2,1,0,1), P0=I",
+            "nx": 5, "ny": 2, "linearization": "cubature", "chunk": C, "group": G,
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": "batch of sequences"}
 
 
@@ -58,8 +62,10 @@ def _oracle_task(args):
     tm = O.FunctionalModel(O.models.CoordinatedTurn(DT), O.MVNSqrt(np.zeros(5), np.linalg.cholesky(Q)))
     om = O.FunctionalModel(O.models.Bearings(S1, S2), O.MVNSqrt(np.zeros(2), np.linalg.cholesky(R)))
     T = ys.shape[0]
+    T = ys.shape[0]
+    nom = O.MVNSqrt(np.repeat(m0[None], T + 1, 0), np.repeat(np.eye(5)[None], T + 1, 0))
     res = O.methods.iterated_smoothing(ys.astype(np.float64), O.MVNSqrt(m0, np.eye(5)), tm, om,
-                                       O.linearization.cubature, None, True, criterion=lambda i, *_: i < N_ITER)
+                                       O.linearization.cubature, nom, True, criterion=lambda i, *_: i < N_ITER)
     return float(np.sum(res.mean))
 
 
@@ -76,8 +82,7 @@ def cpu_sample(lengths, batch, budget_steps):
 
 
 def run_cpu(seqs, processes):
-    from sqrt_parallel_smoothers_gb300.data import BEARINGS_M0
-    tasks = [(y, BEARINGS_M0.copy()) for y in seqs]
+    tasks = [(y, PRIOR_M0.copy()) for y in seqs]
     t0 = time.perf_counter()
     if processes <= 1:
         for t in tasks:
@@ -102,8 +107,7 @@ def reference_arm(args):
     import multiprocessing as mp
     times = []
     with mp.get_context("spawn").Pool(cores) as pool:
-        from sqrt_parallel_smoothers_gb300.data import BEARINGS_M0
-        tasks = [(y, BEARINGS_M0.copy()) for y in seqs]
+        tasks = [(y, PRIOR_M0.copy()) for y in seqs]
         for k in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             pool.map(_oracle_task, tasks, chunksize=1)
@@ -186,15 +190,15 @@ def models(torch, S, dtype):
     return tm, om
 
 
-def make_plan(torch, S, ys, offsets, dtype, chunk=0, group=0, graph=True, profile=False):
+def make_plan(torch, S, ys, offsets, dtype, chunk=0, group=0, graph=True, profile=False, criterion=None):
     tm, om = models(torch, S, dtype)
-    m0 = torch.as_tensor(S.data.BEARINGS_M0, dtype=dtype)
+    m0 = torch.as_tensor(PRIOR_M0, dtype=dtype)
     x0 = S.MVNSqrt(m0, torch.eye(5, dtype=dtype))
-    # init_nominal_trajectory=None: the reference's default start (one filter-smoother pass at
-    # zero means / identity factors, parsmooth/methods.py:63-65), then N_ITER counted calls
-    return S.IteratedSmootherPlan(torch.as_tensor(ys, dtype=dtype), x0, tm, om, S.linearization.cubature, None,
-                                  criterion=S.FixedIterations(N_ITER), offsets=offsets, chunk=chunk, group=group,
-                                  graph=graph, profile=profile)
+    n_states = int(ys.shape[0]) + len(offsets) - 1
+    nom = S.MVNSqrt(m0.expand(n_states, 5).contiguous(), torch.eye(5, dtype=dtype).expand(n_states, 5, 5).contiguous())
+    return S.IteratedSmootherPlan(torch.as_tensor(ys, dtype=dtype), x0, tm, om, S.linearization.cubature, nom,
+                                  criterion=criterion or S.FixedIterations(N_ITER), offsets=offsets, chunk=chunk,
+                                  group=group, graph=graph, profile=profile)
 
 
 def time_plan(torch, plan, steps, warmup, flush=None, sampler=None):
@@ -234,6 +238,49 @@ ALG_BYTES_PER_STEP = {
     "filter_walk": 4 * (60 + 2 + 45),  # ... in, smoothing element out
     "smoother_walk": 4 * (45 + 20),  # smoothing element in, smoothed state out
 }
+
+
+def adjoint_section(torch, S, flush):
+    """Gradient of the batch pseudo-log-likelihood w.r.t. (s1x, s1y, log q, log sigma): bearings model,
+    B = 64 sequences of T = 5000, FP32 tangent-linear filter, checked against central differences
+    (h = 1e-3) of the same filter in FP64."""
+    B, T = 64, 5000
+    batch = S.data.bearings_batch(np.full(B, T), qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=20_000)
+    Q1, _ = S.data.bearings_noise(1.0, QW / QC, SIGMA, DT)
+    theta0 = np.array([S1[0], S1[1], np.log(QC), np.log(SIGMA)])
+    m0 = torch.as_tensor(PRIOR_M0)
+    x0 = S.MVNSqrt(m0, torch.eye(5, dtype=torch.float64))
+    n_states = B * (T + 1)
+    nom = S.MVNSqrt(m0.expand(n_states, 5).contiguous(), torch.eye(5, dtype=torch.float64).expand(n_states, 5, 5))
+
+    def ell_grad(theta, dtype):
+        th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+        ell = S.BearingsLogLikelihood.apply(th, torch.as_tensor(batch["ys"], dtype=dtype), x0, nom, Q1, DT, S2,
+                                            S.linearization.cubature, None, batch["offsets"])
+        ell.backward()
+        return float(ell), th.grad.numpy()
+
+    ell_grad(theta0, torch.float32)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(3):
+        flush.add_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ell32, g32 = ell_grad(theta0, torch.float32)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    h = 1e-3
+    fd = []
+    for k in range(4):
+        e = np.zeros(4)
+        e[k] = h
+        fd.append((ell_grad(theta0 + e, torch.float64)[0] - ell_grad(theta0 - e, torch.float64)[0]) / (2 * h))
+    fd = np.array(fd)
+    rel = np.abs(g32 - fd) / np.abs(fd)
+    return {"B": B, "T": T, "dtype": "f32", "ms": float(np.median(times)) * 1e3, "ell": ell32,
+            "grad": g32.tolist(), "fd_grad_fp64": fd.tolist(), "rel_err": rel.tolist(),
+            "max_rel_err": float(np.max(rel)), "method": "tangent-linear filter, one pass per parameter"}
 
 
 def gpu_arm(args):
@@ -349,19 +396,34 @@ def gpu_arm(args):
     line["fp64_plain"] = {"value": v64, "unit": UNIT, "T": FP64_PLAIN_T, "ms_per_step": float(np.mean(ms64))}
     line["ratio_vs_fp64_plain"] = value / world / v64
 
-    # accuracy: FP32 batched vs FP64 batched (same GPU path, FP64) against the simulated truth
+    # accuracy: FP32 batched vs FP64 batched (same GPU path in FP64, checked against the FP64 oracle in
+    # the tests) against the simulated truth.  "Converged" = the FP64 run meets the reference's default
+    # test (mean squared change <= 1e-6) within the same 10 calls; the FP32 and FP64 RMSEs are compared
+    # on those sequences (undamped Gauss-Newton diverges on some long, strongly manoeuvring tracks).
     plan_acc = make_plan(torch, S, batch["ys"], offsets, torch.float64, graph=False)
     plan_acc.run()
     torch.cuda.synchronize()
     mean64 = plan_acc.mean.cpu().numpy()
     del plan_acc
+    plan_cv = make_plan(torch, S, batch["ys"], offsets, torch.float64, graph=False,
+                        criterion=S.MeanSquaredChange(1e-6, N_ITER))
+    plan_cv.run()
+    torch.cuda.synchronize()
+    conv = (plan_cv._outs[4].cpu().numpy() & 4) == 0
+    del plan_cv
     r32 = position_rmse(mean32, batch["xs"].astype(np.float64), offsets)
     r64 = position_rmse(mean64, batch["xs"].astype(np.float64), offsets)
     rel = np.abs(r32 - r64) / np.maximum(r64, 1e-12)
-    line["accuracy"] = {"rmse_fp32_median": float(np.median(r32)), "rmse_fp64_median": float(np.median(r64)),
-                        "rmse_rel_diff_median": float(np.median(rel)), "rmse_rel_diff_p95": float(np.quantile(rel, 0.95)),
-                        "frac_within_1pct": float(np.mean(rel <= 0.01)),
-                        "max_abs_mean_diff_fp32_vs_fp64": float(np.max(np.abs(mean32 - mean64)))}
+    line["accuracy"] = {"converged_frac_fp64": float(np.mean(conv)),
+                        "rmse_fp32_median_converged": float(np.median(r32[conv])),
+                        "rmse_fp64_median_converged": float(np.median(r64[conv])),
+                        "rmse_rel_diff_median_converged": float(np.median(rel[conv])),
+                        "rmse_rel_diff_max_converged": float(np.max(rel[conv])),
+                        "frac_within_1pct_converged": float(np.mean(rel[conv] <= 0.01)),
+                        "frac_within_1pct_all": float(np.mean(rel <= 0.01)),
+                        "rmse": "position RMSE of smoothed means vs simulated truth, per sequence"}
+
+    line["adjoint"] = adjoint_section(torch, S, flush)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         seqs, tot = cpu_sample(lengths, batch, budget_steps=6000)

@@ -147,6 +147,36 @@ int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void*
                 int32_t* out_iters, uint32_t* out_flags, void* workspace, size_t workspace_bytes,
                 ss_stream_t stream);
 
+/* Forward-mode sensitivities of the pseudo-log-likelihood.
+ * The reference obtains dl/dtheta with jax.grad through its parallel filter
+ * (used in notebooks/experiment_bearing_only_parameter_estimation.ipynb:91).
+ * Here the filter of ss_filter (parsmooth/parallel/_filtering.py:13-61 with
+ * return_loglikelihood) is run in tangent-linear arithmetic: every model
+ * scalar carries up to SS_MAX_TANGENTS derivative directions d(.)/dtheta_k,
+ * given by ss_tangents, and the log-likelihood of each sequence comes back
+ * with its gradient (out_grad, (B, n_dir) double).  Built for
+ * (nx, ny) = (5, 2) and (2, 2) with the extended, cubature and unscented
+ * linearisations. */
+#define SS_MAX_TANGENTS 4
+typedef struct ss_tangents {
+  int32_t n_dir;                      /* 1..SS_MAX_TANGENTS */
+  int32_t reserved;
+  double trans_params[SS_MAX_TANGENTS][4];  /* d(transition params)/dtheta_k */
+  double obs_params[SS_MAX_TANGENTS][4];    /* d(observation params)/dtheta_k */
+  const void* trans_matrix;           /* (n_dir, nx, nx) or NULL for zero, device */
+  const void* obs_matrix;             /* (n_dir, ny, nx) or NULL */
+  const void* trans_noise_mean;       /* (n_dir, nx) or NULL */
+  const void* trans_noise_chol;       /* (n_dir, nx, nx) or NULL */
+  const void* obs_noise_mean;         /* (n_dir, ny) or NULL */
+  const void* obs_noise_chol;         /* (n_dir, ny, ny) or NULL */
+} ss_tangents;
+
+int ss_filter_grad_workspace_bytes(const ss_problem* p, size_t* bytes);
+int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void* ys, const void* m0,
+                   const void* L0, int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
+                   double* out_ell, double* out_grad, void* workspace, size_t workspace_bytes,
+                   ss_stream_t stream);
+
 /* Instrumentation (no counterpart in the reference, which has no tracing):
  * a counter of kernels launched by this library, and per-kernel CUDA-event
  * timing.  While profiling is enabled every launch is bracketed by two events

@@ -10,10 +10,11 @@ __version__ = "1.0.0"
 
 from ._base import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsModel
 from .methods import (filtering, smoothing, filter_smoother, iterated_smoothing, linearize, FixedIterations,
-                      MeanSquaredChange, IteratedSmootherPlan)
+                      MeanSquaredChange, IteratedSmootherPlan, ModelTangent, filter_loglikelihood_grad,
+                      BearingsLogLikelihood)
 from . import linearization, models, data
 
 __all__ = ["MVNSqrt", "MVNStandard", "FunctionalModel", "ConditionalMomentsModel", "filtering", "smoothing",
            "filter_smoother", "iterated_smoothing", "linearize", "FixedIterations", "MeanSquaredChange",
-           "IteratedSmootherPlan",
+           "IteratedSmootherPlan", "ModelTangent", "filter_loglikelihood_grad", "BearingsLogLikelihood",
            "linearization", "models", "data"]

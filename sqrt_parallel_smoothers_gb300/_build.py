@@ -66,7 +66,7 @@ def build(verbose=False, jobs=None):
     jobs = jobs or max(1, min(len(todo), os.cpu_count() or 1))
     if todo:
         # the largest units first so the tail of the parallel build is short
-        todo.sort(key=lambda so: ("f64" not in so[0], "_5" not in so[0]))
+        todo.sort(key=lambda so: ("grad" not in so[0], "f64" not in so[0], "_5_" not in so[0]))
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
             for log in ex.map(lambda so: _compile(so[0], so[1], verbose), todo):
                 if verbose and log:

@@ -14,10 +14,11 @@ SS_F32, SS_F64 = 0, 1
 SS_LIN_EXTENDED, SS_LIN_CUBATURE, SS_LIN_UNSCENTED, SS_LIN_GAUSS_HERMITE = 0, 1, 2, 3
 SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS = 0, 1, 2
 SS_MAX_GH_ORDER = 8
+SS_MAX_TANGENTS = 4
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
-            "ss_filter", "ss_smooth", "ss_iterated", "ss_launch_count", "ss_profile_enable", "ss_profile_read",
-            "ss_profile_reset")
+            "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",
+            "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
 
 
 class SSModel(ctypes.Structure):
@@ -34,6 +35,15 @@ class SSProblem(ctypes.Structure):
                 ("group", ctypes.c_int32), ("reserved", ctypes.c_int32), ("transition", SSModel),
                 ("observation", SSModel), ("batch", ctypes.c_int64), ("total_steps", ctypes.c_int64),
                 ("max_len", ctypes.c_int64), ("offsets", ctypes.c_void_p)]
+
+
+class SSTangents(ctypes.Structure):
+    _fields_ = [("n_dir", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("trans_params", (ctypes.c_double * 4) * SS_MAX_TANGENTS),
+                ("obs_params", (ctypes.c_double * 4) * SS_MAX_TANGENTS),
+                ("trans_matrix", ctypes.c_void_p), ("obs_matrix", ctypes.c_void_p),
+                ("trans_noise_mean", ctypes.c_void_p), ("trans_noise_chol", ctypes.c_void_p),
+                ("obs_noise_mean", ctypes.c_void_p), ("obs_noise_chol", ctypes.c_void_p)]
 
 
 _lock = threading.Lock()
@@ -65,6 +75,9 @@ def load():
         lib.ss_smooth.argtypes = [PP, P, P, P, P, P, P, P, ctypes.c_size_t, P]
         lib.ss_iterated.argtypes = [PP, P, P, P, ctypes.c_int32, P, P, ctypes.c_int32, ctypes.c_double,
                                     P, P, P, P, P, P, ctypes.c_size_t, P]
+        lib.ss_filter_grad_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
+        lib.ss_filter_grad.argtypes = [PP, ctypes.POINTER(SSTangents), P, P, P, ctypes.c_int32, P, P, P, P, P,
+                                       ctypes.c_size_t, P]
         lib.ss_profile_enable.argtypes = [ctypes.c_int]
         lib.ss_profile_read.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         for name in EXPORTED:

@@ -1,0 +1,4 @@
+// Forward-mode gradient instantiations for dtype f64, (nx, ny) = (5, 2).
+#include "ss_grad.cuh"
+
+SS_INST_GRAD(double, f64, 5, 2)

@@ -19,6 +19,19 @@ namespace ss {
   int run_f64_##NX##_##NY(const Call& c);
 SS_FOR_DIMS(SS_DECL)
 #undef SS_DECL
+#define SS_DECL(NX, NY)                      \
+  int grad_f32_##NX##_##NY(const Call& c);   \
+  int grad_f64_##NX##_##NY(const Call& c);
+SS_FOR_GRAD_DIMS(SS_DECL)
+#undef SS_DECL
+
+static RunFn find_grad(int dtype, int nx, int ny) {
+#define SS_CASE(NX, NY) \
+  if (nx == NX && ny == NY) return dtype == SS_F32 ? grad_f32_##NX##_##NY : grad_f64_##NX##_##NY;
+  SS_FOR_GRAD_DIMS(SS_CASE)
+#undef SS_CASE
+  return nullptr;
+}
 
 static RunFn find_run(int dtype, int nx, int ny) {
 #define SS_CASE(NX, NY) \
@@ -307,6 +320,53 @@ int ss_smooth(const ss_problem* p, const void* filt_m, const void* filt_L, const
   c.ws_bytes = workspace_bytes;
   c.stream = reinterpret_cast<cudaStream_t>(stream);
   return dispatch(c);
+}
+
+int ss_filter_grad_workspace_bytes(const ss_problem* p, size_t* bytes) {
+  if (bytes == nullptr) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  RunFn f = find_grad(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_WORKSPACE;
+  c.p = p;
+  c.ws_bytes_out = bytes;
+  c.prior_per_sequence = 1;  // the larger of the two prior layouts
+  return f(c);
+}
+
+int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void* ys, const void* m0,
+                   const void* L0, int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
+                   double* out_ell, double* out_grad, void* workspace, size_t workspace_bytes,
+                   ss_stream_t stream) {
+  if (p == nullptr || tangents == nullptr || m0 == nullptr || L0 == nullptr || out_ell == nullptr ||
+      out_grad == nullptr)
+    return SS_ERR_INVALID;
+  if (p->total_steps > 0 && ys == nullptr) return SS_ERR_INVALID;
+  if ((nominal_m == nullptr) != (nominal_L == nullptr)) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  RunFn f = find_grad(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_FILTER;
+  c.p = p;
+  c.tangents = tangents;
+  c.ys = ys;
+  c.m0 = m0;
+  c.L0 = L0;
+  c.prior_per_sequence = prior_per_sequence;
+  c.nom_m = nominal_m;
+  c.nom_L = nominal_L;
+  c.out_ell = out_ell;
+  c.out_grad = out_grad;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return f(c);
 }
 
 int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void* L0,

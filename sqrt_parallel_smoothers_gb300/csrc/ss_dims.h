@@ -7,5 +7,7 @@
   X(3, 1) X(3, 2) X(3, 3) \
   X(4, 1) X(4, 2) X(4, 3) \
   X(5, 1) X(5, 2) X(5, 3)
+// (nx, ny) pairs with forward-mode gradient kernels (ss_filter_grad).
+#define SS_FOR_GRAD_DIMS(X) X(2, 2) X(5, 2)
 #define SS_MAX_NX 5
 #define SS_MAX_NY 3

@@ -236,22 +236,33 @@ SS_DEV void matvec_t(const R (&A)[M][N], const R (&x)[M], R (&y)[N]) {
 // them with 16-byte vector accesses.
 
 template <typename R>
-struct Vec16;
+struct Vec16 {  // scalar types without a 16-byte vector form are moved element by element
+  static constexpr int n = 1;
+  static constexpr bool vec = false;
+};
 template <>
 struct Vec16<float> {
   typedef float4 type;
   static constexpr int n = 4;
+  static constexpr bool vec = true;
 };
 template <>
 struct Vec16<double> {
   typedef double2 type;
   static constexpr int n = 2;
+  static constexpr bool vec = true;
 };
 
 template <typename R, int N>
 struct Padded {
   static constexpr int n = ((N + Vec16<R>::n - 1) / Vec16<R>::n) * Vec16<R>::n;
 };
+
+// Read-only cached load for built-in scalars, plain load otherwise.
+SS_DEV float ldg(const float* p) { return __ldg(p); }
+SS_DEV double ldg(const double* p) { return __ldg(p); }
+template <typename R>
+SS_DEV R ldg(const R* p) { return *p; }
 
 // Global side must be 16-byte aligned (records sit at 16-byte multiples in a
 // 256-byte aligned workspace); the register side is copied element by element.
@@ -262,20 +273,30 @@ SS_DEV double2 vec_from(const double* s) { return make_double2(s[0], s[1]); }
 
 template <typename R, int N>
 SS_DEV void load_rec(const R* __restrict__ src, R (&dst)[Padded<R, N>::n]) {
-  typedef typename Vec16<R>::type V;
-  constexpr int W = Vec16<R>::n;
-  const V* s = reinterpret_cast<const V*>(src);
-  SS_UNROLL
-  for (int k = 0; k < Padded<R, N>::n / W; ++k) vec_to(__ldg(s + k), dst + k * W);
+  if constexpr (Vec16<R>::vec) {
+    typedef typename Vec16<R>::type V;
+    constexpr int W = Vec16<R>::n;
+    const V* s = reinterpret_cast<const V*>(src);
+    SS_UNROLL
+    for (int k = 0; k < Padded<R, N>::n / W; ++k) vec_to(__ldg(s + k), dst + k * W);
+  } else {
+    SS_UNROLL
+    for (int k = 0; k < N; ++k) dst[k] = src[k];
+  }
 }
 
 template <typename R, int N>
 SS_DEV void store_rec(R* __restrict__ dst, const R (&src)[Padded<R, N>::n]) {
-  typedef typename Vec16<R>::type V;
-  constexpr int W = Vec16<R>::n;
-  V* d = reinterpret_cast<V*>(dst);
-  SS_UNROLL
-  for (int k = 0; k < Padded<R, N>::n / W; ++k) d[k] = vec_from(src + k * W);
+  if constexpr (Vec16<R>::vec) {
+    typedef typename Vec16<R>::type V;
+    constexpr int W = Vec16<R>::n;
+    V* d = reinterpret_cast<V*>(dst);
+    SS_UNROLL
+    for (int k = 0; k < Padded<R, N>::n / W; ++k) d[k] = vec_from(src + k * W);
+  } else {
+    SS_UNROLL
+    for (int k = 0; k < N; ++k) dst[k] = src[k];
+  }
 }
 
 // Copy helpers between flat records and matrices.

@@ -4,7 +4,7 @@
 // Python, so models are C++ functors selected by id.  Each functor evaluates
 // f(x) and its Jacobian (the Jacobian is only used by the extended method).
 #pragma once
-#include "ss_la.cuh"
+#include "ss_dual.cuh"
 #include "../../include/sqrtsmooth.h"
 
 namespace ss {
@@ -15,6 +15,19 @@ SS_DEV float ss_cos(float x) { return cosf(x); }
 SS_DEV double ss_cos(double x) { return cos(x); }
 SS_DEV float ss_atan2(float y, float x) { return atan2f(y, x); }
 SS_DEV double ss_atan2(double y, double x) { return atan2(y, x); }
+template <typename T, int NT>
+SS_DEV Dual<T, NT> ss_sin(const Dual<T, NT>& a) { return chain(a, ss_sin(a.v), ss_cos(a.v)); }
+template <typename T, int NT>
+SS_DEV Dual<T, NT> ss_cos(const Dual<T, NT>& a) { return chain(a, ss_cos(a.v), -ss_sin(a.v)); }
+template <typename T, int NT>
+SS_DEV Dual<T, NT> ss_atan2(const Dual<T, NT>& y, const Dual<T, NT>& x) {
+  Dual<T, NT> r;
+  r.v = ss_atan2(y.v, x.v);
+  const T inv = T(1) / (x.v * x.v + y.v * y.v);
+  SS_UNROLL
+  for (int k = 0; k < NT; ++k) r.d[k] = (x.v * y.d[k] - y.v * x.d[k]) * inv;
+  return r;
+}
 
 // Parameters of one model as the kernels see them (device pointers / scalars).
 template <typename R>
@@ -136,19 +149,19 @@ struct RuleArgs {
 };
 
 template <typename R>
-SS_DEV R rule_ut(const RuleArgs& r, int i);
+SS_DEV R rule_ut(const RuleArgs& r, int i) { return R(r.ut_d[i]); }
 template <>
 SS_DEV float rule_ut<float>(const RuleArgs& r, int i) { return r.ut_f[i]; }
 template <>
 SS_DEV double rule_ut<double>(const RuleArgs& r, int i) { return r.ut_d[i]; }
 template <typename R>
-SS_DEV R rule_gh_root(const RuleArgs& r, int i);
+SS_DEV R rule_gh_root(const RuleArgs& r, int i) { return R(r.gh_root_d[i]); }
 template <>
 SS_DEV float rule_gh_root<float>(const RuleArgs& r, int i) { return r.gh_root_f[i]; }
 template <>
 SS_DEV double rule_gh_root<double>(const RuleArgs& r, int i) { return r.gh_root_d[i]; }
 template <typename R>
-SS_DEV R rule_gh_w(const RuleArgs& r, int i);
+SS_DEV R rule_gh_w(const RuleArgs& r, int i) { return R(r.gh_w_d[i]); }
 template <>
 SS_DEV float rule_gh_w<float>(const RuleArgs& r, int i) { return r.gh_w_f[i]; }
 template <>

@@ -258,9 +258,9 @@ template <typename R, int D>
 SS_DEV void load_noise(const R* qm, const R* qL, R (&m)[D], R (&L)[D][D]) {
   SS_UNROLL
   for (int i = 0; i < D; ++i) {
-    m[i] = __ldg(qm + i);
+    m[i] = ldg(qm + i);
     SS_UNROLL
-    for (int j = 0; j < D; ++j) L[i][j] = __ldg(qL + i * D + j);
+    for (int j = 0; j < D; ++j) L[i][j] = ldg(qL + i * D + j);
   }
 }
 
@@ -504,7 +504,10 @@ __global__ void __launch_bounds__(128) filter_walk_kernel(ScanArgs<R> a) {
   State<R, NX> s;
   load_st<R, NX>(a.fst[1] + j * Q::ST_P, s);
   SElem<R, NX> acc;
-  double ll = 0.0;
+  constexpr int NC = 1 + Tangents<R>::n;   // log-likelihood value (+ tangents), FP64
+  double ll[NC];
+  SS_UNROLL
+  for (int k = 0; k < NC; ++k) ll[k] = 0.0;
   for (int64_t t = t0; t < t1; ++t) {
     Lin<R, NX, NY> l;
     load_lin<R, NX, NY>(a.lin + (base + t) * Q::LIN_P, l);
@@ -518,11 +521,17 @@ __global__ void __launch_bounds__(128) filter_walk_kernel(ScanArgs<R> a) {
       store_se<R, NX>(a.selem + (base + t) * Q::SE_P, se);
       if (t == t0) acc = se; else smoother_fold<R, NX>(acc, se);
     }
-    ll += (double)filter_update<R, NX, NY>(s, l, y, X, mp);
+    double c[NC];
+    to_components(filter_update<R, NX, NY>(s, l, y, X, mp), c);
+    SS_UNROLL
+    for (int k = 0; k < NC; ++k) ll[k] += c[k];
     if (a.filt_m != nullptr) store_traj<R, NX>(a.filt_m, a.filt_L, base + i + t + 1, s);
   }
   if (a.emit_smoother) store_se<R, NX>(a.ssum[1] + j * Q::SE_P, acc);
-  if (a.ll_chunk != nullptr) a.ll_chunk[j] = ll;
+  if (a.ll_chunk != nullptr) {
+    SS_UNROLL
+    for (int k = 0; k < NC; ++k) a.ll_chunk[j * NC + k] = ll[k];
+  }
   if (t1 == a.g.off[i + 1] - base) store_st<R, NX>(a.fT + i * Q::ST_P, s);
 }
 
@@ -673,16 +682,24 @@ __global__ void __launch_bounds__(128) smoother_walk_kernel(ScanArgs<R> a) {
 // ----------------------------------------------------------------------------- finishing kernels
 
 // Per-sequence log-likelihood: sum of chunk partials plus the constant
-// -T ny/2 log(2 pi), all in FP64.
-static __global__ void ll_reduce_kernel(Geo g, int ny, const double* __restrict__ ll_chunk,
-                                 double* __restrict__ out, uint32_t* flags) {
+// -T ny/2 log(2 pi), all in FP64.  With NC > 1 the chunk partials carry
+// tangent components too; component c goes to grad[i * grad_ld + grad_col + c - 1].
+static __global__ void ll_reduce_kernel(Geo g, int ny, int NC, const double* __restrict__ ll_chunk,
+                                        double* __restrict__ out, double* __restrict__ grad, int grad_ld,
+                                        int grad_col, uint32_t* flags) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.B) return;
   const int64_t T = g.off[i + 1] - g.off[i];
-  double s = -0.5 * (double)T * (double)ny * 1.8378770664093453;  // log(2 pi)
-  for (int64_t j = g.lvl[1][i]; j < g.lvl[1][i + 1]; ++j) s += ll_chunk[j];
-  out[i] = s;
-  if (flags != nullptr && !isfinite(s)) atomicOr(flags + i, 2u);
+  for (int c = 0; c < NC; ++c) {
+    double s = (c == 0) ? -0.5 * (double)T * (double)ny * 1.8378770664093453 : 0.0;  // log(2 pi)
+    for (int64_t j = g.lvl[1][i]; j < g.lvl[1][i + 1]; ++j) s += ll_chunk[j * NC + c];
+    if (c == 0) {
+      out[i] = s;
+      if (flags != nullptr && !isfinite(s)) atomicOr(flags + i, 2u);
+    } else if (grad != nullptr) {
+      grad[i * grad_ld + grad_col + (c - 1)] = s;
+    }
+  }
 }
 
 // After one filter-smoother call in tolerance mode: count the call, stop

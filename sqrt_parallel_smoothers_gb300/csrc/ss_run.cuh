@@ -3,7 +3,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "ss_pipeline.cuh"
+#include "ss_staged.cuh"
 
 namespace ss {
 
@@ -34,6 +34,9 @@ struct Call {
   void* out_m;
   void* out_L;
   double* out_ell;
+  double* out_grad;   // (B, grad_ld) gradient output; this run writes column grad_col
+  int32_t grad_ld;
+  int32_t grad_col;
   int32_t n_iter;
   double tol;
   int32_t* out_iters;
@@ -41,6 +44,7 @@ struct Call {
   void* ws;
   size_t ws_bytes;
   cudaStream_t stream;
+  const ss_tangents* tangents;  // forward-mode directions of the model scalars (gradient runs)
 };
 
 typedef int (*RunFn)(const Call&);
@@ -86,7 +90,7 @@ inline int make_layout(const ss_problem& p, Layout& y) {
     y.sst[l] = take(sizeof(R) * Q::ST_P * (size_t)y.items[l]);
   }
   y.fT = take(sizeof(R) * Q::ST_P * (size_t)B);
-  y.ll = take(sizeof(double) * (size_t)y.items[1]);
+  y.ll = take(sizeof(double) * (size_t)y.items[1] * (1 + Tangents<R>::n));
   y.mse = take(sizeof(double) * (size_t)B);
   y.active = take(sizeof(int32_t) * (size_t)B);
   y.iters = take(sizeof(int32_t) * (size_t)B);
@@ -154,17 +158,30 @@ inline void record_event(cudaEvent_t e, cudaStream_t st) {
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block > 0 ? (n + block - 1) / block : 1); }
 
 // Lin-kernel dispatch over the model pair and method.
-template <typename R, int NX, int NY, class TF, class OF>
-inline int launch_lin_method(const LinArgs<R>& a, int method, cudaStream_t st) {
-  const unsigned grid = grid_for(a.total, 128);
-  switch (method) {
-    case SS_LIN_EXTENDED: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_EXTENDED><<<grid, 128, 0, st>>>(a)); break;
-    case SS_LIN_CUBATURE: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_CUBATURE><<<grid, 128, 0, st>>>(a)); break;
-    case SS_LIN_UNSCENTED: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_UNSCENTED><<<grid, 128, 0, st>>>(a)); break;
-    case SS_LIN_GAUSS_HERMITE: SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, SS_LIN_GAUSS_HERMITE><<<grid, 128, 0, st>>>(a)); break;
-    default: return SS_ERR_UNSUPPORTED;
+template <typename R, int NX, int NY, class TF, class OF, int METHOD>
+inline int launch_lin_one(const LinArgs<R>& a, cudaStream_t st) {
+  const unsigned grid = grid_for(a.total, STAGED_BLOCK);
+  if constexpr (Vec16<R>::vec) {
+    constexpr int sm = (int)StagedSmem<R, NX, NY>::lin;
+    cudaFuncSetAttribute(lin_staged_kernel<R, NX, NY, TF, OF, METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    SS_LAUNCH("lin", st, lin_staged_kernel<R, NX, NY, TF, OF, METHOD><<<grid, STAGED_BLOCK, sm, st>>>(a));
+  } else {
+    SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, METHOD><<<grid, 128, 0, st>>>(a));
   }
   return SS_OK;
+}
+
+template <typename R, int NX, int NY, class TF, class OF>
+inline int launch_lin_method(const LinArgs<R>& a, int method, cudaStream_t st) {
+  switch (method) {
+    case SS_LIN_EXTENDED: return launch_lin_one<R, NX, NY, TF, OF, SS_LIN_EXTENDED>(a, st);
+    case SS_LIN_CUBATURE: return launch_lin_one<R, NX, NY, TF, OF, SS_LIN_CUBATURE>(a, st);
+    case SS_LIN_UNSCENTED: return launch_lin_one<R, NX, NY, TF, OF, SS_LIN_UNSCENTED>(a, st);
+    case SS_LIN_GAUSS_HERMITE:
+      if constexpr (Tangents<R>::n == 0) return launch_lin_one<R, NX, NY, TF, OF, SS_LIN_GAUSS_HERMITE>(a, st);
+      else return SS_ERR_UNSUPPORTED;
+    default: return SS_ERR_UNSUPPORTED;
+  }
 }
 
 template <int NX>
@@ -191,12 +208,23 @@ inline int launch_lin_obs(const LinArgs<R>& a, int ok, int method, cudaStream_t 
 template <typename R, int NX, int NY>
 inline int launch_lin(const LinArgs<R>& a, int tk, int ok, int method, cudaStream_t st) {
   if (a.total == 0) return SS_OK;
-  if (tk == SS_MODEL_LINEAR) return launch_lin_obs<R, NX, NY, LinearFn<R, NX, NX>>(a, ok, method, st);
-  if constexpr (ct_ok<NX>()) {
-    if (tk == SS_MODEL_COORDINATED_TURN)
-      return launch_lin_obs<R, NX, NY, CoordinatedTurnFn<R, NX, NX>>(a, ok, method, st);
+  if constexpr (Tangents<R>::n > 0) {
+    // gradient runs: the bearings pair at (5, 2) and linear pairs only
+    if constexpr (ct_ok<NX>() && bearings_ok<NX, NY>()) {
+      if (tk == SS_MODEL_COORDINATED_TURN && ok == SS_MODEL_BEARINGS)
+        return launch_lin_method<R, NX, NY, CoordinatedTurnFn<R, NX, NX>, BearingsFn<R, NX, NY>>(a, method, st);
+    }
+    if (tk == SS_MODEL_LINEAR && ok == SS_MODEL_LINEAR)
+      return launch_lin_method<R, NX, NY, LinearFn<R, NX, NX>, LinearFn<R, NX, NY>>(a, method, st);
+    return SS_ERR_UNSUPPORTED;
+  } else {
+    if (tk == SS_MODEL_LINEAR) return launch_lin_obs<R, NX, NY, LinearFn<R, NX, NX>>(a, ok, method, st);
+    if constexpr (ct_ok<NX>()) {
+      if (tk == SS_MODEL_COORDINATED_TURN)
+        return launch_lin_obs<R, NX, NY, CoordinatedTurnFn<R, NX, NX>>(a, ok, method, st);
+    }
+    return SS_ERR_UNSUPPORTED;
   }
-  return SS_ERR_UNSUPPORTED;
 }
 
 template <typename R, int DIN, int DOUT, class Fn>
@@ -264,6 +292,16 @@ struct Runner {
     la.total = p.total_steps;
     la.tm = model_args<R>(p.transition);
     la.om = model_args<R>(p.observation);
+    if constexpr (Tangents<R>::n > 0) {
+      if (c.tangents != nullptr) {
+        for (int dir = 0; dir < c.tangents->n_dir && dir < Tangents<R>::n; ++dir) {
+          for (int k = 0; k < 4; ++k) {
+            la.tm.p[k].d[dir] = c.tangents->trans_params[dir][k];
+            la.om.p[k].d[dir] = c.tangents->obs_params[dir][k];
+          }
+        }
+      }
+    }
     la.tq_m = static_cast<const R*>(p.transition.noise_mean);
     la.tq_L = static_cast<const R*>(p.transition.noise_chol);
     la.oq_m = static_cast<const R*>(p.observation.noise_mean);
@@ -297,11 +335,24 @@ struct Runner {
   }
 
   int filter_pass(bool emit_smoother) {
-    SS_LAUNCH("filter_leaf", st, filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    const unsigned g1 = grid_for(y.items[1], STAGED_BLOCK);
+    if constexpr (Vec16<R>::vec) {
+      constexpr int sm = (int)StagedSmem<R, NX, NY>::leaf;
+      cudaFuncSetAttribute(filter_leaf_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      SS_LAUNCH("filter_leaf", st, filter_leaf_staged_kernel<R, NX, NY><<<g1, STAGED_BLOCK, sm, st>>>(sa));
+    } else {
+      SS_LAUNCH("filter_leaf", st, filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    }
     int rc = filter_scan();
     if (rc) return rc;
     sa.emit_smoother = emit_smoother ? 1 : 0;
-    SS_LAUNCH("filter_walk", st, filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    if constexpr (Vec16<R>::vec) {
+      constexpr int sm = (int)StagedSmem<R, NX, NY>::fwalk;
+      cudaFuncSetAttribute(filter_walk_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      SS_LAUNCH("filter_walk", st, filter_walk_staged_kernel<R, NX, NY><<<g1, STAGED_BLOCK, sm, st>>>(sa));
+    } else {
+      SS_LAUNCH("filter_walk", st, filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    }
     return SS_OK;
   }
 
@@ -313,7 +364,14 @@ struct Runner {
     for (int l = y.L - 1; l >= 1; --l) {
       SS_LAUNCH("smoother_down", st, smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
     }
-    SS_LAUNCH("smoother_walk", st, smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    if constexpr (Vec16<R>::vec) {
+      constexpr int sm = (int)StagedSmem<R, NX, NY>::swalk;
+      cudaFuncSetAttribute(smoother_walk_staged_kernel<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      SS_LAUNCH("smoother_walk", st,
+                smoother_walk_staged_kernel<R, NX><<<grid_for(y.items[1], STAGED_BLOCK), STAGED_BLOCK, sm, st>>>(sa));
+    } else {
+      SS_LAUNCH("smoother_walk", st, smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    }
     return SS_OK;
   }
 
@@ -328,7 +386,7 @@ struct Runner {
     rc = filter_pass(false);
     if (rc) return rc;
     if (c.out_ell) {
-      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, nullptr));
+      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, 1 + Tangents<R>::n, at<double>(y.ll), c.out_ell, c.out_grad, c.grad_ld, c.grad_col, nullptr));
     }
     return SS_OK;
   }
@@ -401,7 +459,7 @@ struct Runner {
       sa.ll_chunk = at<double>(y.ll);
       rc = filter_pass(false);
       if (rc) return rc;
-      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, at<double>(y.ll), c.out_ell, c.out_flags));
+      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, 1 + Tangents<R>::n, at<double>(y.ll), c.out_ell, nullptr, 0, 0, c.out_flags));
     }
     if (c.out_iters || (c.out_flags && tol_mode)) {
       if (!tol_mode) {

@@ -1,0 +1,287 @@
+// The four per-step kernels of the filter-smoother pass with their global
+// traffic staged through shared memory (see ss_stage.cuh): the per-step
+// linearisation, the chunk fold of filtering elements, the chunk Kalman walk
+// and the chunk RTS walk.  Used for float and double; the per-lane variants
+// in ss_pipeline.cuh remain for dual numbers.
+#pragma once
+#include "ss_pipeline.cuh"
+#include "ss_stage.cuh"
+
+namespace ss {
+
+template <typename R, int NX, int NY>
+SS_DEV void pack_lin(R (&r)[Rec<R, NX, NY>::LIN_P], const Lin<R, NX, NY>& l) {
+  typedef Rec<R, NX, NY> Q;
+  int o = 0;
+  pack<R, NX, NX>(r, o, l.F); o += NX * NX;
+  pack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
+  pack_vec<R, NX>(r, o, l.bq); o += NX;
+  pack<R, NY, NX>(r, o, l.H); o += NY * NX;
+  pack<R, NY, NY>(r, o, l.cR); o += NY * NY;
+  pack_vec<R, NY>(r, o, l.c); o += NY;
+  SS_UNROLL
+  for (int k = Q::LIN; k < Q::LIN_P; ++k) r[k] = R(0);
+}
+
+template <typename R, int NX, int NY>
+SS_DEV void unpack_lin(const R (&r)[Rec<R, NX, NY>::LIN_P], Lin<R, NX, NY>& l) {
+  int o = 0;
+  unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
+  unpack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
+  unpack_vec<R, NX>(r, o, l.bq); o += NX;
+  unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
+  unpack<R, NY, NY>(r, o, l.cR); o += NY * NY;
+  unpack_vec<R, NY>(r, o, l.c);
+}
+
+template <typename R, int NX>
+SS_DEV void pack_se(R (&r)[Rec<R, NX, 1>::SE_P], const SElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
+  int o = 0;
+  pack_vec<R, NX>(r, o, e.g); o += NX;
+  pack<R, NX, NX>(r, o, e.E); o += NX * NX;
+  pack<R, NX, NX>(r, o, e.D); o += NX * NX;
+  SS_UNROLL
+  for (int k = Q::SE; k < Q::SE_P; ++k) r[k] = R(0);
+}
+
+template <typename R, int NX>
+SS_DEV void unpack_se(const R (&r)[Rec<R, NX, 1>::SE_P], SElem<R, NX>& e) {
+  int o = 0;
+  unpack_vec<R, NX>(r, o, e.g); o += NX;
+  unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
+  unpack<R, NX, NX>(r, o, e.D);
+}
+
+constexpr int STAGED_BLOCK = 128;
+constexpr int STAGED_WARPS = STAGED_BLOCK / 32;
+
+// Dynamic shared memory (bytes) of each staged kernel.
+template <typename R, int NX, int NY>
+struct StagedSmem {
+  typedef Rec<R, NX, NY> Q;
+  static constexpr size_t lin = sizeof(R) * STAGED_WARPS * StageTile<R, Q::LIN>::WARP_ELEMS;
+  static constexpr size_t leaf = 2 * lin;
+  static constexpr size_t fwalk = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS;
+  static constexpr size_t swalk = sizeof(R) * STAGED_WARPS *
+                                  (2 * StageTile<R, Q::SE>::WARP_ELEMS + 32 * ((NX * NX) | 1));
+};
+
+template <typename R>
+SS_DEV R* warp_smem(unsigned char* raw, size_t warp_elems) {
+  return reinterpret_cast<R*>(raw) + (threadIdx.x >> 5) * warp_elems;
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int NX, int NY, class TF, class OF, int METHOD>
+__global__ void __launch_bounds__(STAGED_BLOCK) lin_staged_kernel(LinArgs<R> a) {
+  typedef Rec<R, NX, NY> Q;
+  extern __shared__ __align__(16) unsigned char ss_smem[];
+  R* tile = warp_smem<R>(ss_smem, StageTile<R, Q::LIN>::WARP_ELEMS);
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool work = k < a.total;
+  int64_t i = 0;
+  if (work) {
+    i = find_seq(a.off, a.B, k);
+    if (a.active != nullptr && a.active[i] == 0) work = false;
+  }
+  R rec[Q::LIN_P];
+  if (work) {
+    const int64_t t = k - a.off[i];
+    const int64_t s = a.off[i] + i + t;
+    Lin<R, NX, NY> l;
+    {
+      TF f;
+      f.init(a.tm);
+      R m[NX], C[NX][NX], qm[NX], qL[NX][NX];
+      load_nominal<R, NX>(a.nom_m, a.nom_L, s, m, C);
+      load_noise<R, NX>(a.tq_m, a.tq_L, qm, qL);
+      linearize<R, NX, NX, TF, METHOD>(f, m, C, qm, qL, a.rule, a.slr_form, l.F, l.cQ, l.bq);
+    }
+    if (a.trans_only) {
+      SS_UNROLL
+      for (int r = 0; r < NY; ++r) {
+        l.c[r] = R(0);
+        SS_UNROLL
+        for (int jj = 0; jj < NX; ++jj) l.H[r][jj] = R(0);
+        SS_UNROLL
+        for (int jj = 0; jj < NY; ++jj) l.cR[r][jj] = R(0);
+      }
+    } else {
+      OF h;
+      h.init(a.om);
+      R m[NX], C[NX][NX], qm[NY], qL[NY][NY];
+      load_nominal<R, NX>(a.nom_m, a.nom_L, s + 1, m, C);
+      load_noise<R, NY>(a.oq_m, a.oq_L, qm, qL);
+      linearize<R, NX, NY, OF, METHOD>(h, m, C, qm, qL, a.rule, a.slr_form, l.H, l.cR, l.c);
+    }
+    pack_lin<R, NX, NY>(rec, l);
+  }
+  stage_store<R, Q::LIN>(tile, rec, work ? a.out + k * Q::LIN_P : nullptr);
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int NX, int NY>
+__global__ void __launch_bounds__(STAGED_BLOCK) filter_leaf_staged_kernel(ScanArgs<R> a) {
+  typedef Rec<R, NX, NY> Q;
+  typedef StageTile<R, Q::LIN> TL;
+  extern __shared__ __align__(16) unsigned char ss_smem[];
+  R* tiles = warp_smem<R>(ss_smem, 2 * TL::WARP_ELEMS);
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool work = j < a.g.lvl[1][a.g.B];
+  int64_t i = 0, t0 = 0, t1 = 0;
+  if (work) {
+    chunk_of(a.g, j, i, t0, t1);
+    if (seq_inactive(a.active, i)) work = false;
+  }
+  const int n = work ? (int)(t1 - t0) : 0;
+  const int64_t first = work ? a.g.off[i] + t0 : 0;
+  stage_load_async<R, Q::LIN>(n > 0 ? a.lin + first * Q::LIN_P : nullptr, tiles);
+  cp_async_commit();
+  FElem<R, NX> acc;
+  for (int s = 0; s < a.g.C; ++s) {
+    if (!__any_sync(FULL_MASK, s < n)) break;
+    stage_load_async<R, Q::LIN>(s + 1 < n ? a.lin + (first + s + 1) * Q::LIN_P : nullptr,
+                                tiles + ((s + 1) & 1) * TL::WARP_ELEMS);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    if (s < n) {
+      R rec[Q::LIN_P];
+      stage_read<R, Q::LIN>(tiles + (s & 1) * TL::WARP_ELEMS, rec);
+      Lin<R, NX, NY> l;
+      unpack_lin<R, NX, NY>(rec, l);
+      R y[NY];
+      SS_UNROLL
+      for (int k = 0; k < NY; ++k) y[k] = a.ys[(first + s) * NY + k];
+      if (s == 0) {
+        filter_element<R, NX, NY>(l, y, acc);
+      } else {
+        FElem<R, NX> e;
+        filter_element<R, NX, NY>(l, y, e);
+        filter_combine<R, NX>(acc, e);
+      }
+    }
+    __syncwarp();
+  }
+  cp_async_wait<0>();
+  if (work) store_fe<R, NX>(a.fsum[1] + j * Q::FE_P, acc);
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int NX, int NY>
+__global__ void __launch_bounds__(STAGED_BLOCK) filter_walk_staged_kernel(ScanArgs<R> a) {
+  typedef Rec<R, NX, NY> Q;
+  typedef StageTile<R, Q::LIN> TL;
+  typedef StageTile<R, Q::SE> TS;
+  extern __shared__ __align__(16) unsigned char ss_smem[];
+  R* tiles = warp_smem<R>(ss_smem, 2 * TL::WARP_ELEMS);
+  R* stile = reinterpret_cast<R*>(ss_smem) + STAGED_WARPS * 2 * TL::WARP_ELEMS + (threadIdx.x >> 5) * TS::WARP_ELEMS;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool work = j < a.g.lvl[1][a.g.B];
+  int64_t i = 0, t0 = 0, t1 = 0;
+  if (work) {
+    chunk_of(a.g, j, i, t0, t1);
+    if (seq_inactive(a.active, i)) work = false;
+  }
+  const int n = work ? (int)(t1 - t0) : 0;
+  const int64_t base = work ? a.g.off[i] : 0;
+  const int64_t first = base + t0;
+  State<R, NX> s;
+  if (work) load_st<R, NX>(a.fst[1] + j * Q::ST_P, s);
+  stage_load_async<R, Q::LIN>(n > 0 ? a.lin + first * Q::LIN_P : nullptr, tiles);
+  cp_async_commit();
+  SElem<R, NX> acc;
+  double ll = 0.0;
+  for (int k = 0; k < a.g.C; ++k) {
+    if (!__any_sync(FULL_MASK, k < n)) break;
+    stage_load_async<R, Q::LIN>(k + 1 < n ? a.lin + (first + k + 1) * Q::LIN_P : nullptr,
+                                tiles + ((k + 1) & 1) * TL::WARP_ELEMS);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    R srec[Q::SE_P];
+    if (k < n) {
+      R rec[Q::LIN_P];
+      stage_read<R, Q::LIN>(tiles + (k & 1) * TL::WARP_ELEMS, rec);
+      Lin<R, NX, NY> l;
+      unpack_lin<R, NX, NY>(rec, l);
+      R y[NY];
+      SS_UNROLL
+      for (int q = 0; q < NY; ++q) y[q] = a.ys[(first + k) * NY + q];
+      R X[2 * NX][2 * NX], mp[NX];
+      SElem<R, NX> se;
+      smoother_element<R, NX>(l.F, l.cQ, l.bq, s, se, X, mp);
+      if (a.emit_smoother) {
+        pack_se<R, NX>(srec, se);
+        if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
+      }
+      ll += (double)filter_update<R, NX, NY>(s, l, y, X, mp);
+      if (a.filt_m != nullptr) store_traj<R, NX>(a.filt_m, a.filt_L, first + i + k + 1, s);
+    }
+    if (a.emit_smoother)
+      stage_store<R, Q::SE>(stile, srec, k < n ? a.selem + (first + k) * Q::SE_P : nullptr);
+    __syncwarp();
+  }
+  cp_async_wait<0>();
+  if (work) {
+    if (a.emit_smoother) store_se<R, NX>(a.ssum[1] + j * Q::SE_P, acc);
+    if (a.ll_chunk != nullptr) a.ll_chunk[j] = ll;
+    if (t1 == a.g.off[i + 1] - base) store_st<R, NX>(a.fT + i * Q::ST_P, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+template <typename R, int NX>
+__global__ void __launch_bounds__(STAGED_BLOCK) smoother_walk_staged_kernel(ScanArgs<R> a) {
+  typedef Rec<R, NX, 1> Q;
+  typedef StageTile<R, Q::SE> TS;
+  constexpr int LW = (NX * NX) | 1;
+  extern __shared__ __align__(16) unsigned char ss_smem[];
+  R* tiles = warp_smem<R>(ss_smem, 2 * TS::WARP_ELEMS);
+  R* otile = reinterpret_cast<R*>(ss_smem) + STAGED_WARPS * 2 * TS::WARP_ELEMS + (threadIdx.x >> 5) * 32 * LW;
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool work = j < a.g.lvl[1][a.g.B];
+  int64_t i = 0, t0 = 0, t1 = 0;
+  if (work) chunk_of(a.g, j, i, t0, t1);
+  const int64_t base = work ? a.g.off[i] : 0;
+  if (work && seq_inactive(a.active, i)) {
+    for (int64_t t = t0; t < t1; ++t) copy_state<R, NX>(a, base + i + t);
+    work = false;
+  }
+  const int n = work ? (int)(t1 - t0) : 0;
+  State<R, NX> s;
+  if (work) load_st<R, NX>(a.sst[1] + j * Q::ST_P, s);
+  // step k handles t = t1 - 1 - k
+  stage_load_async<R, Q::SE>(n > 0 ? a.selem + (base + t1 - 1) * Q::SE_P : nullptr, tiles);
+  cp_async_commit();
+  for (int k = 0; k < a.g.C; ++k) {
+    if (!__any_sync(FULL_MASK, k < n)) break;
+    stage_load_async<R, Q::SE>(k + 1 < n ? a.selem + (base + t1 - 2 - k) * Q::SE_P : nullptr,
+                               tiles + ((k + 1) & 1) * TS::WARP_ELEMS);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncwarp();
+    R mrow[NX], Lrow[NX * NX];
+    const int64_t st = base + i + t1 - 1 - k;
+    if (k < n) {
+      R rec[Q::SE_P];
+      stage_read<R, Q::SE>(tiles + (k & 1) * TS::WARP_ELEMS, rec);
+      SElem<R, NX> e;
+      unpack_se<R, NX>(rec, e);
+      smoother_apply<R, NX>(s, e);
+      accumulate_change<R, NX>(a, i, st, s);
+      SS_UNROLL
+      for (int r = 0; r < NX; ++r) {
+        mrow[r] = s.m[r];
+        SS_UNROLL
+        for (int c = 0; c < NX; ++c) Lrow[r * NX + c] = (c <= r) ? s.L[r][c] : R(0);
+      }
+    }
+    stage_store_words<R, NX>(otile, mrow, k < n ? a.out_m + st * NX : nullptr);
+    stage_store_words<R, NX * NX>(otile, Lrow, k < n ? a.out_L + st * NX * NX : nullptr);
+  }
+  cp_async_wait<0>();
+}
+
+}  // namespace ss

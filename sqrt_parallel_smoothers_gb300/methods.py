@@ -374,6 +374,45 @@ def _(m, L, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg, which):
     return m.new_empty((n, d_out, nx)), m.new_empty((n, d_out, d_out)), m.new_empty((n, d_out))
 
 
+@torch.library.custom_op("sqrtsmooth::filter_grad", mutates_args=())
+def _filter_grad_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L0: torch.Tensor,
+                    nom_m: Optional[torch.Tensor], nom_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor],
+                    t_qm: torch.Tensor, t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor,
+                    o_qL: torch.Tensor, d_tmat: Optional[torch.Tensor], d_omat: Optional[torch.Tensor],
+                    d_tqm: Optional[torch.Tensor], d_tqL: Optional[torch.Tensor], d_oqm: Optional[torch.Tensor],
+                    d_oqL: Optional[torch.Tensor], d_params: List[float], icfg: List[int], fcfg: List[float]
+                    ) -> Tuple[torch.Tensor, torch.Tensor]:
+    B, n_dir, per = icfg[10], icfg[14], icfg[13]
+    dev = ys.device
+    pr = _problem(icfg, fcfg, ys.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    lib = _lib.load()
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.ss_filter_grad_workspace_bytes(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
+    ws = _workspace(nbytes.value, dev)
+    tg = _lib.SSTangents()
+    tg.n_dir = n_dir
+    for d in range(n_dir):
+        for k in range(4):
+            tg.trans_params[d][k] = d_params[d * 8 + k]
+            tg.obs_params[d][k] = d_params[d * 8 + 4 + k]
+    tg.trans_matrix, tg.obs_matrix = _ptr(d_tmat), _ptr(d_omat)
+    tg.trans_noise_mean, tg.trans_noise_chol = _ptr(d_tqm), _ptr(d_tqL)
+    tg.obs_noise_mean, tg.obs_noise_chol = _ptr(d_oqm), _ptr(d_oqL)
+    ell = torch.empty((B,), dtype=torch.float64, device=dev)
+    grad = torch.empty((B, n_dir), dtype=torch.float64, device=dev)
+    _lib.check(lib.ss_filter_grad(_lib.ctypes.byref(pr), _lib.ctypes.byref(tg), _ptr(ys), _ptr(m0), _ptr(L0), per,
+                                  _ptr(nom_m), _ptr(nom_L), _ptr(ell), _ptr(grad), _ptr(ws), nbytes.value,
+                                  _stream(dev)))
+    return ell, grad
+
+
+@_filter_grad_op.register_fake
+def _(ys, offsets, m0, L0, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, d_tmat, d_omat, d_tqm, d_tqL,
+      d_oqm, d_oqL, d_params, icfg, fcfg):
+    B, n_dir = icfg[10], icfg[14]
+    return ys.new_empty((B,), dtype=torch.float64), ys.new_empty((B, n_dir), dtype=torch.float64)
+
+
 # ----------------------------------------------------------------------------- public API
 
 def _check_common(x0, parallel, method):
@@ -660,3 +699,99 @@ class IteratedSmootherPlan:
         """The smoothed trajectory in the caller's layout."""
         lay, nx = self.layout, self.nx
         return MVNSqrt(lay.unpack_states(self.mean, (nx,)), lay.unpack_states(self.chol, (nx, nx)))
+
+
+# ----------------------------------------------------------------------------- gradients
+
+class ModelTangent:
+    """Derivative of one model's scalars with respect to one parameter direction.
+
+    ``params``: d(model params)/dtheta (``dt`` of CoordinatedTurn, ``(s1x, s1y, s2x, s2y)`` of
+    Bearings); ``matrix``: d A/dtheta of a LinearModel; ``noise_mean`` / ``noise_chol``: derivative
+    of the noise mean and (lower) square root.  Missing entries are zero."""
+
+    def __init__(self, params=None, matrix=None, noise_mean=None, noise_chol=None):
+        self.params = list(params) if params is not None else [0.0] * 4
+        self.params += [0.0] * (4 - len(self.params))
+        self.matrix, self.noise_mean, self.noise_chol = matrix, noise_mean, noise_chol
+
+
+def filter_loglikelihood_grad(observations, x0, transition_model, observation_model, linearization_method,
+                              nominal_trajectory, directions, *, lengths=None, offsets=None, chunk=0, group=0,
+                              slr_form=0):
+    """Log-likelihood of the parallel filter and its derivatives along parameter directions.
+
+    ``directions``: list (at most 4) of ``(transition ModelTangent, observation ModelTangent)``.
+    The filter (parsmooth/parallel/_filtering.py:13-61, return_loglikelihood) runs in
+    tangent-linear arithmetic, one pass per direction, on the GPU.  Returns ``(ell, grad)``
+    (FP64), ``grad[..., k] = d ell / d theta_k``; per sequence for batches."""
+    method = _check_common(x0, True, linearization_method)
+    if nominal_trajectory is not None:
+        are_inputs_compatible(x0, nominal_trajectory)
+    n_dir = len(directions)
+    if not 1 <= n_dir <= _lib.SS_MAX_TANGENTS:
+        raise ValueError(f"1..{_lib.SS_MAX_TANGENTS} directions are supported")
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_qL = _model_tensors(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, L0, per = _prior(x0, lay, nx)
+    nm, nL = _nominal(nominal_trajectory, lay, nx)
+
+    def stack(get, shape):
+        vals = [get(d) for d in directions]
+        if all(v is None for v in vals):
+            return None
+        return torch.stack([torch.zeros(shape, dtype=lay.dtype, device=dev) if v is None
+                            else _as(v, lay.dtype, dev).reshape(shape) for v in vals]).contiguous()
+
+    ny = lay.ny
+    d_tmat = stack(lambda d: d[0].matrix, (nx, nx))
+    d_omat = stack(lambda d: d[1].matrix, (ny, nx))
+    d_tqm = stack(lambda d: d[0].noise_mean, (nx,))
+    d_tqL = stack(lambda d: d[0].noise_chol, (nx, nx))
+    d_oqm = stack(lambda d: d[1].noise_mean, (ny,))
+    d_oqL = stack(lambda d: d[1].noise_chol, (ny, ny))
+    d_params = []
+    for d in directions:
+        d_params += [float(v) for v in d[0].params] + [float(v) for v in d[1].params]
+    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, [per, n_dir])
+    ell, grad = torch.ops.sqrtsmooth.filter_grad(lay.ys, lay.offsets, m0, L0, nm, nL, t_mat, t_qm, t_qL, o_mat,
+                                                 o_qm, o_qL, d_tmat, d_omat, d_tqm, d_tqL, d_oqm, d_oqL, d_params,
+                                                 icfg, _fcfg(method, fn_t, fn_o))
+    return lay.per_sequence(ell), lay.per_sequence(grad)
+
+
+class BearingsLogLikelihood(torch.autograd.Function):
+    """Pseudo-log-likelihood of the bearings model as a differentiable function of
+    ``theta = (s1x, s1y, log q, log sigma)``.
+
+    ``Q(q) = q * Q1`` (``Q1`` the coordinated-turn noise at q = 1) and ``R = sigma^2 I``; the
+    second sensor, the prior and the nominal trajectory are fixed.  The forward pass runs the
+    GPU filter in tangent-linear arithmetic and keeps ``d ell / d theta``; backward is the
+    vector-Jacobian product.  ``ell`` is summed over the batch."""
+
+    @staticmethod
+    def forward(ctx, theta, observations, x0, nominal, Q1, dt, s2, method, lengths, offsets):
+        from .models import Bearings, CoordinatedTurn
+        th = theta.detach().double().cpu()
+        s1 = (float(th[0]), float(th[1]))
+        q, sigma = float(torch.exp(th[2])), float(torch.exp(th[3]))
+        cQ = torch.linalg.cholesky(torch.as_tensor(Q1, dtype=torch.float64) * q)
+        cR = sigma * torch.eye(2, dtype=torch.float64)
+        tm = FunctionalModel(CoordinatedTurn(dt), MVNSqrt(torch.zeros(5, dtype=torch.float64), cQ))
+        om = FunctionalModel(Bearings(s1, s2), MVNSqrt(torch.zeros(2, dtype=torch.float64), cR))
+        dirs = [(ModelTangent(), ModelTangent(params=[1, 0, 0, 0])),
+                (ModelTangent(), ModelTangent(params=[0, 1, 0, 0])),
+                (ModelTangent(noise_chol=0.5 * cQ), ModelTangent()),
+                (ModelTangent(), ModelTangent(noise_chol=cR))]
+        ell, grad = filter_loglikelihood_grad(observations, x0, tm, om, method, nominal, dirs, lengths=lengths,
+                                              offsets=offsets)
+        ctx.save_for_backward(grad.reshape(-1, 4).sum(0).to(theta.dtype))
+        return ell.sum().to(theta.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (g,) = ctx.saved_tensors
+        return (grad_out * g.to(grad_out.device),) + (None,) * 9
