@@ -304,6 +304,12 @@ def gpu_arm(args):
     lengths = S.data.ragged_lengths(args.batch, seed=0)
     batch = S.data.bearings_batch(lengths, qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=rank * args.batch)
     offsets = batch["offsets"]
+    tuning = None
+    if args.chunk == 0 and not args.no_autotune:
+        from sqrt_parallel_smoothers_gb300 import autotune
+        key = autotune.signature(5, 2, "f32", lengths, "cubature")
+        args.chunk, args.group, tuning = autotune.tune(
+            lambda c, g: make_plan(torch, S, batch["ys"], offsets, torch.float32, c, g), key=key)
     plan = make_plan(torch, S, batch["ys"], offsets, torch.float32, args.chunk, args.group)
     C = args.chunk or 16
     G = args.group or 8
@@ -348,6 +354,8 @@ def gpu_arm(args):
                                                        "bearings experiment)",
             "config": workload_config(args.batch, lengths, C, G), "e2e": e2e, "gpu_launches": int(launches),
             "clocks": clocks}
+    if tuning is not None:
+        line["config"]["autotune_ms"] = tuning
 
     if args.only_main:
         print(json.dumps(line), flush=True)
@@ -449,6 +457,7 @@ def main():
     ap.add_argument("--group", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-main", action="store_true", help="time the FP32 batched smoother only")
+    ap.add_argument("--no-autotune", action="store_true", help="use the default chunk/group (16, 8)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -75,7 +75,7 @@ int run_grad(const Call& c) {
   }
   if (c.ws == nullptr || c.ws_bytes < g.bytes) return SS_ERR_WORKSPACE;
   const ss_tangents* tg = c.tangents;
-  if (tg == nullptr || tg->n_dir < 1 || tg->n_dir > GRAD_NT) return SS_ERR_INVALID;
+  if (tg == nullptr || tg->n_dir < 1 || tg->n_dir > SS_MAX_TANGENTS) return SS_ERR_INVALID;
   char* w = static_cast<char*>(c.ws);
   cudaStream_t st = c.stream;
   const int nd = tg->n_dir;

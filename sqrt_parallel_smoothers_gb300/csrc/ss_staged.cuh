@@ -86,6 +86,8 @@ __global__ void __launch_bounds__(STAGED_BLOCK) lin_staged_kernel(LinArgs<R> a) 
     if (a.active != nullptr && a.active[i] == 0) work = false;
   }
   R rec[Q::LIN_P];
+  SS_UNROLL
+  for (int q = 0; q < Q::LIN_P; ++q) rec[q] = R(0);  // idle lanes stage zeros (never stored)
   if (work) {
     const int64_t t = k - a.off[i];
     const int64_t s = a.off[i] + i + t;
@@ -201,6 +203,8 @@ __global__ void __launch_bounds__(STAGED_BLOCK) filter_walk_staged_kernel(ScanAr
     cp_async_wait<1>();
     __syncwarp();
     R srec[Q::SE_P];
+    SS_UNROLL
+    for (int q = 0; q < Q::SE_P; ++q) srec[q] = R(0);
     if (k < n) {
       R rec[Q::LIN_P];
       stage_read<R, Q::LIN>(tiles + (k & 1) * TL::WARP_ELEMS, rec);
@@ -263,6 +267,10 @@ __global__ void __launch_bounds__(STAGED_BLOCK) smoother_walk_staged_kernel(Scan
     cp_async_wait<1>();
     __syncwarp();
     R mrow[NX], Lrow[NX * NX];
+    SS_UNROLL
+    for (int q = 0; q < NX; ++q) mrow[q] = R(0);
+    SS_UNROLL
+    for (int q = 0; q < NX * NX; ++q) Lrow[q] = R(0);
     const int64_t st = base + i + t1 - 1 - k;
     if (k < n) {
       R rec[Q::SE_P];

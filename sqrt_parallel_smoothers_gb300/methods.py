@@ -788,8 +788,8 @@ class BearingsLogLikelihood(torch.autograd.Function):
                 (ModelTangent(), ModelTangent(noise_chol=cR))]
         ell, grad = filter_loglikelihood_grad(observations, x0, tm, om, method, nominal, dirs, lengths=lengths,
                                               offsets=offsets)
-        ctx.save_for_backward(grad.reshape(-1, 4).sum(0).to(theta.dtype))
-        return ell.sum().to(theta.dtype)
+        ctx.save_for_backward(grad.reshape(-1, 4).sum(0).to(device=theta.device, dtype=theta.dtype))
+        return ell.sum().to(device=theta.device, dtype=theta.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):

@@ -230,25 +230,31 @@ def test_default_criterion_linear_exact():
 
 
 def test_default_criterion_bearings():
-    """Slowly converging bearings case: the call count may differ by one where the
-    mean squared change crosses 1e-6 within rounding of the two implementations."""
+    """Slowly converging bearings case: the device test must stop where the mean squared
+    change of the means crosses 1e-6 (checked on the oracle's own iterates; FP64 rounding
+    may move a slow crossing by a call or two)."""
     (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
     w = S.data.bearings_workload(200, seed=3)
     ys = w["ys"].astype(float)
     nom = (np.repeat(w["m0"][None], 201, 0), np.repeat(np.eye(5)[None], 201, 0))
-    calls = []
+    mse = []
 
     def crit(i, prev, cur):
-        calls.append(i)
-        return O.methods.default_criterion(i, prev, cur)
+        mse.append(float(np.mean((np.asarray(prev.mean) - np.asarray(cur.mean)) ** 2)))
+        return mse[-1] > 1e-6
 
     O.methods.iterated_smoothing(ys, O.MVNSqrt(w["m0"], np.eye(5)), ot, oo, O.linearization.extended,
                                  O.MVNSqrt(*nom), True, criterion=crit)
     res, info = S.iterated_smoothing(torch.as_tensor(ys), S.MVNSqrt(torch.as_tensor(w["m0"]),
                                      torch.eye(5, dtype=torch.float64)), gt, go, S.linearization.extended,
                                      S.MVNSqrt(torch.as_tensor(nom[0]), torch.as_tensor(nom[1])), return_info=True)
-    assert abs(int(info["iterations"]) - max(calls)) <= 1
+    k = int(info["iterations"])
     assert int(info["flags"]) == 0
+    assert abs(k - len(mse)) <= 3
+    if k <= len(mse):
+        assert mse[k - 1] <= 4e-6            # the oracle is (nearly) converged where the GPU stopped
+    if k >= 2:
+        assert mse[min(k, len(mse)) - 2] >= 1e-6 / 4   # and was not converged one call earlier
     assert torch.isfinite(res.mean).all()
 
 
