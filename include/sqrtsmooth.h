@@ -147,6 +147,23 @@ int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void*
                 int32_t* out_iters, uint32_t* out_flags, void* workspace, size_t workspace_bytes,
                 ss_stream_t stream);
 
+/* ss_iterated without a workspace argument, for callers that cannot allocate
+ * device memory (no counterpart in the reference, which lets JAX/XLA allocate).
+ * Scratch comes from a fixed array of SS_NOALLOC_SCRATCH_BYTES inside the
+ * library's device image, held on every GPU that loads the library until the
+ * process exits.  Problems whose ss_workspace_bytes exceed it are rejected
+ * with SS_ERR_WORKSPACE.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress, with that device current); make that
+ * first call before any stream capture.  All calls share the one array, so
+ * calls whose GPU work overlaps (other streams, other threads) race and must
+ * be serialised by the caller; a call fully rewrites what it reads, so no
+ * clearing between calls is needed.  Allocates nothing. */
+#define SS_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int ss_iterated_noalloc(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+                        int32_t prior_per_sequence, const void* init_m, const void* init_L,
+                        int32_t n_iter, double tol, void* out_m, void* out_L, double* out_ell,
+                        int32_t* out_iters, uint32_t* out_flags, ss_stream_t stream);
+
 /* Forward-mode sensitivities of the pseudo-log-likelihood.
  * The reference obtains dl/dtheta with jax.grad through its parallel filter
  * (used in notebooks/experiment_bearing_only_parameter_estimation.ipynb:91).
