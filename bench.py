@@ -238,6 +238,9 @@ ALG_BYTES_PER_STEP = {
     "filter_walk": 4 * (60 + 2 + 45),  # ... in, smoothing element out
     "smoother_walk": 4 * (45 + 20),  # smoothing element in, smoothed state out
 }
+# DRAM bytes (read + write) per timestep of each kernel, from one ncu capture of this workload
+# (profiles/staged_kernels_bearings_b1024_c16g8.md: bytes of one launch / 1,101,870 timesteps)
+TRAFFIC_BYTES_PER_STEP = {"lin": 354, "filter_leaf": 319, "filter_walk": 517, "smoother_walk": 363}
 
 
 def adjoint_section(torch, S, flush):
@@ -258,7 +261,7 @@ def adjoint_section(torch, S, flush):
         ell = S.BearingsLogLikelihood.apply(th, torch.as_tensor(batch["ys"], dtype=dtype), x0, nom, Q1, DT, S2,
                                             S.linearization.cubature, None, batch["offsets"])
         ell.backward()
-        return float(ell), th.grad.numpy()
+        return float(ell.detach()), th.grad.numpy()
 
     ell_grad(theta0, torch.float32)
     torch.cuda.synchronize()
@@ -391,7 +394,8 @@ def gpu_arm(args):
     if alg is not None:
         achieved = alg * sum_T / (kern[dom]["avg_ms"] * 1e-3) / 1e9
         line["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                            "frac": achieved / hbm_peak, "traffic": None,
+                            "frac": achieved / hbm_peak,
+                            "traffic": TRAFFIC_BYTES_PER_STEP[dom] * sum_T if dom in TRAFFIC_BYTES_PER_STEP else None,
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
                             "alg_bytes_per_launch": alg * sum_T}
     line["kernels"] = kern

@@ -109,10 +109,12 @@ SS_DEV bool ss_isfinite(const Dual<T, NT>& a) { return ss_isfinite(a.v); }
 template <typename T>
 struct Tangents {
   static constexpr int n = 0;
+  using scalar = T;
 };
 template <typename T, int NT>
 struct Tangents<Dual<T, NT>> {
   static constexpr int n = NT;
+  using scalar = T;  // the arithmetic precision of the value and tangents
 };
 
 // Value and tangents of a scalar as doubles (for FP64 accumulation).

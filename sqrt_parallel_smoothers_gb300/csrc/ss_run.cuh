@@ -308,7 +308,7 @@ struct Runner {
     la.oq_L = static_cast<const R*>(p.observation.noise_chol);
     rc = fill_rule(p, la.rule);
     if (rc) return rc;
-    la.slr_form = slr_form_of(p, sizeof(R) == 4);
+    la.slr_form = slr_form_of(p, sizeof(typename Tangents<R>::scalar) == 4);
     la.out = at<R>(y.lin);
     return SS_OK;
   }
@@ -483,7 +483,7 @@ struct Runner {
     a.q_L = static_cast<const R*>(mdl.noise_chol);
     int rc = fill_rule(p, a.rule);
     if (rc) return rc;
-    a.slr_form = slr_form_of(p, sizeof(R) == 4);
+    a.slr_form = slr_form_of(p, sizeof(typename Tangents<R>::scalar) == 4);
     a.F = static_cast<R*>(c.pt_F);
     a.chol = static_cast<R*>(c.pt_chol);
     a.b = static_cast<R*>(c.pt_b);

@@ -229,33 +229,34 @@ def test_default_criterion_linear_exact():
     assert_rel(res.mean, ref.mean, F64_TOL, "mean")
 
 
-def test_default_criterion_bearings():
-    """Slowly converging bearings case: the device test must stop where the mean squared
-    change of the means crosses 1e-6 (checked on the oracle's own iterates; FP64 rounding
-    may move a slow crossing by a call or two)."""
+@pytest.mark.parametrize("method", ["extended", "cubature"])
+def test_default_criterion_bearings(method):
+    """Bearings case that takes several calls: the device test must stop on the same call as
+    the reference's default test (mean squared change of the means > 1e-6).  The prior is the
+    simulator's initial state, so Gauss-Newton converges without wandering and the crossing of
+    1e-6 has a wide margin on both sides (oracle history seed 3: extended 8.4e-6 -> 3.5e-9 on
+    call 5, cubature 1.9e-4 -> 8.7e-8 on call 7)."""
     (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
     w = S.data.bearings_workload(200, seed=3)
     ys = w["ys"].astype(float)
-    nom = (np.repeat(w["m0"][None], 201, 0), np.repeat(np.eye(5)[None], 201, 0))
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    nom = (np.repeat(m0[None], 201, 0), np.repeat(np.eye(5)[None], 201, 0))
     mse = []
 
     def crit(i, prev, cur):
         mse.append(float(np.mean((np.asarray(prev.mean) - np.asarray(cur.mean)) ** 2)))
         return mse[-1] > 1e-6
 
-    O.methods.iterated_smoothing(ys, O.MVNSqrt(w["m0"], np.eye(5)), ot, oo, O.linearization.extended,
-                                 O.MVNSqrt(*nom), True, criterion=crit)
-    res, info = S.iterated_smoothing(torch.as_tensor(ys), S.MVNSqrt(torch.as_tensor(w["m0"]),
-                                     torch.eye(5, dtype=torch.float64)), gt, go, S.linearization.extended,
+    ref = O.methods.iterated_smoothing(ys, O.MVNSqrt(m0, np.eye(5)), ot, oo, getattr(O.linearization, method),
+                                       O.MVNSqrt(*nom), True, criterion=crit)
+    assert mse[-1] < 1e-7 and mse[-2] > 4e-6          # the margin the comparison relies on
+    res, info = S.iterated_smoothing(torch.as_tensor(ys), S.MVNSqrt(torch.as_tensor(m0),
+                                     torch.eye(5, dtype=torch.float64)), gt, go,
+                                     getattr(S.linearization, method),
                                      S.MVNSqrt(torch.as_tensor(nom[0]), torch.as_tensor(nom[1])), return_info=True)
-    k = int(info["iterations"])
     assert int(info["flags"]) == 0
-    assert abs(k - len(mse)) <= 3
-    if k <= len(mse):
-        assert mse[k - 1] <= 4e-6            # the oracle is (nearly) converged where the GPU stopped
-    if k >= 2:
-        assert mse[min(k, len(mse)) - 2] >= 1e-6 / 4   # and was not converged one call earlier
-    assert torch.isfinite(res.mean).all()
+    assert int(info["iterations"]) == len(mse)
+    assert_rel(res.mean, ref.mean, 1e-8, "mean")
 
 
 def test_tolerance_mode_in_batch_stops_sequences_independently():
