@@ -24,6 +24,11 @@ SS_FOR_DIMS(SS_DECL)
   int grad_f64_##NX##_##NY(const Call& c);
 SS_FOR_GRAD_DIMS(SS_DECL)
 #undef SS_DECL
+#define SS_DECL(NX, NY)                      \
+  int dense_f32_##NX##_##NY(const Call& c);  \
+  int dense_f64_##NX##_##NY(const Call& c);
+SS_FOR_DENSE_DIMS(SS_DECL)
+#undef SS_DECL
 
 static RunFn find_grad(int dtype, int nx, int ny) {
 #define SS_CASE(NX, NY) \
@@ -37,6 +42,10 @@ static RunFn find_run(int dtype, int nx, int ny) {
 #define SS_CASE(NX, NY) \
   if (nx == NX && ny == NY) return dtype == SS_F32 ? run_f32_##NX##_##NY : run_f64_##NX##_##NY;
   SS_FOR_DIMS(SS_CASE)
+#undef SS_CASE
+#define SS_CASE(NX, NY) \
+  if (nx == NX && ny == NY) return dtype == SS_F32 ? dense_f32_##NX##_##NY : dense_f64_##NX##_##NY;
+  SS_FOR_DENSE_DIMS(SS_CASE)
 #undef SS_CASE
   return nullptr;
 }

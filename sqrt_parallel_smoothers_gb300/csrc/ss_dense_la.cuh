@@ -1,0 +1,461 @@
+// Warp-cooperative dense linear algebra for the large-state path.
+//
+// A matrix lives in the warp's slice of shared memory, row-major, with a row
+// stride of an odd number of 16-byte units: eight lanes that each touch their
+// own row with a 16-byte access then hit eight distinct bank groups, and a
+// warp that reads one row (a broadcast) or one column (consecutive
+// addresses) is conflict-free as well.  Every operation hands row r of its
+// result to lane r % 32 (rows 32..63 are a lane's second slot), computes that
+// row in registers and writes it back, then synchronises the warp.
+//
+// Shapes are compile-time; column counts of blocks that are written inside a
+// larger matrix are multiples of the 16-byte vector width, so no write spills
+// into a neighbouring block.  No operation may write a matrix it reads.
+#pragma once
+#include <utility>
+
+#include "ss_la.cuh"
+
+namespace ss {
+namespace dense {
+
+template <typename R>
+struct Vec;
+template <>
+struct Vec<float> {
+  static constexpr int n = 4;
+  float v[4];
+};
+template <>
+struct Vec<double> {
+  static constexpr int n = 2;
+  double v[2];
+};
+
+SS_DEV Vec<float> ld16(const float* p) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  Vec<float> r;
+  r.v[0] = t.x;
+  r.v[1] = t.y;
+  r.v[2] = t.z;
+  r.v[3] = t.w;
+  return r;
+}
+SS_DEV Vec<double> ld16(const double* p) {
+  const double2 t = *reinterpret_cast<const double2*>(p);
+  Vec<double> r;
+  r.v[0] = t.x;
+  r.v[1] = t.y;
+  return r;
+}
+SS_DEV void st16(float* p, const Vec<float>& v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+SS_DEV void st16(double* p, const Vec<double>& v) {
+  *reinterpret_cast<double2*>(p) = make_double2(v.v[0], v.v[1]);
+}
+
+// Row geometry of an N-column matrix: n = padded row length (whole 16-byte
+// units), ld = row stride (an odd number of 16-byte units).
+template <typename R, int N>
+struct Pad {
+  static constexpr int W = Vec<R>::n;
+  static constexpr int n = (N + W - 1) / W * W;
+  static constexpr int q = n / W;
+  static constexpr int ld = ((q & 1) ? q : q + 1) * W;
+};
+
+SS_DEV int lane_id() { return threadIdx.x & 31; }
+
+// Zero n elements (n a multiple of the vector width, p 16-byte aligned).
+template <typename R>
+SS_DEV void zero(R* p, int n) {
+  Vec<R> z;
+  SS_UNROLL
+  for (int u = 0; u < Vec<R>::n; ++u) z.v[u] = R(0);
+  for (int q = lane_id() * Vec<R>::n; q < n; q += 32 * Vec<R>::n) st16(p + q, z);
+  __syncwarp();
+}
+
+template <typename R, int COLS, int LD>
+SS_DEV void load_row(const R* M, int r, R (&x)[Pad<R, COLS>::n]) {
+  constexpr int W = Vec<R>::n;
+  SS_UNROLL
+  for (int j = 0; j < Pad<R, COLS>::n; j += W) {
+    const Vec<R> v = ld16(M + r * LD + j);
+    SS_UNROLL
+    for (int u = 0; u < W; ++u) x[j + u] = (j + u < COLS) ? v.v[u] : R(0);
+  }
+}
+
+template <typename R, int COLS, int LD>
+SS_DEV void store_row(R* M, int r, const R (&x)[Pad<R, COLS>::n]) {
+  constexpr int W = Vec<R>::n;
+  SS_UNROLL
+  for (int j = 0; j < Pad<R, COLS>::n; j += W) {
+    Vec<R> v;
+    SS_UNROLL
+    for (int u = 0; u < W; ++u) v.v[u] = (j + u < COLS) ? x[j + u] : R(0);
+    st16(M + r * LD + j, v);
+  }
+}
+
+// ----------------------------------------------------------------------------- tria
+
+// M <- [L 0] = M Q, Q orthogonal, L lower triangular with a non-negative
+// diagonal: Householder reflections from the right (Golub & Van Loan,
+// Algorithm 5.1.1, with Parlett's formula for the sign-free reflector, so the
+// diagonal comes out non-negative without a second pass).  The pivot lane
+// publishes each reflector in vb (>= Pad<COLS>::n + W elements, 16-byte
+// aligned); pivots are processed in blocks of eight so that every register
+// index stays compile-time.
+template <typename R, int ROWS, int COLS, int LD>
+struct Tria {
+  static constexpr int W = Vec<R>::n;
+  static constexpr int CP = Pad<R, COLS>::n;
+  static constexpr int NS = (ROWS + 31) / 32;
+  static_assert(ROWS <= COLS, "tria needs rows <= cols");
+  static_assert(LD >= CP, "row stride too small");
+
+  template <int J0>
+  static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
+    const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
+    for (int p = J0; p < pend; ++p) {
+      if (lane == (p & 31)) {
+        const int ps = p >> 5;
+        R x0 = R(0), sig = R(0);
+        SS_UNROLL
+        for (int j = J0; j < CP; ++j) {
+          R xj = row[0][j];
+          if constexpr (NS > 1) {
+            if (ps == 1) xj = row[1][j];
+          }
+          if (j == p) x0 = xj;
+          const R vj = (j > p && j < COLS) ? xj : R(0);
+          sig += vj * vj;
+          vb[j] = vj;
+        }
+        const R nrm = ss_sqrt(x0 * x0 + sig);
+        const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
+        const R vv = v0 * v0 + sig;
+        vb[p] = v0;
+        vb[CP] = (vv > R(0)) ? R(2) / vv : R(0);
+        SS_UNROLL
+        for (int s = 0; s < NS; ++s) {
+          if (s == ps) {
+            SS_UNROLL
+            for (int j = J0; j < CP; ++j) {
+              if (j == p) row[s][j] = nrm;
+              else if (j > p) row[s][j] = R(0);
+            }
+          }
+        }
+      }
+      __syncwarp();
+      const R tau = vb[CP];
+      R d[NS];
+      SS_UNROLL
+      for (int s = 0; s < NS; ++s) d[s] = R(0);
+      SS_UNROLL
+      for (int j = J0; j < CP; j += W) {
+        const Vec<R> v = ld16(vb + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) {
+          SS_UNROLL
+          for (int s = 0; s < NS; ++s) d[s] += row[s][j + u] * v.v[u];
+        }
+      }
+      SS_UNROLL
+      for (int s = 0; s < NS; ++s) {
+        const int r = lane + 32 * s;
+        d[s] = (r > p && r < ROWS) ? tau * d[s] : R(0);
+      }
+      SS_UNROLL
+      for (int j = J0; j < CP; j += W) {
+        const Vec<R> v = ld16(vb + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) {
+          SS_UNROLL
+          for (int s = 0; s < NS; ++s) row[s][j + u] -= d[s] * v.v[u];
+        }
+      }
+      __syncwarp();
+    }
+  }
+
+  template <int... B>
+  static SS_DEV void blocks(R (&row)[NS][CP], R* vb, int lane, std::integer_sequence<int, B...>) {
+    (block<8 * B>(row, vb, lane), ...);
+  }
+
+  static SS_DEV void run(R* M, R* vb) {
+    const int lane = lane_id();
+    R row[NS][CP];
+    SS_UNROLL
+    for (int s = 0; s < NS; ++s) {
+      const int r = lane + 32 * s;
+      if (r < ROWS) {
+        load_row<R, COLS, LD>(M, r, row[s]);
+      } else {
+        SS_UNROLL
+        for (int j = 0; j < CP; ++j) row[s][j] = R(0);
+      }
+    }
+    blocks(row, vb, lane, std::make_integer_sequence<int, (ROWS + 7) / 8>{});
+    SS_UNROLL
+    for (int s = 0; s < NS; ++s) {
+      const int r = lane + 32 * s;
+      if (r < ROWS) store_row<R, COLS, LD>(M, r, row[s]);
+    }
+    __syncwarp();
+  }
+};
+
+template <typename R, int ROWS, int COLS, int LD>
+SS_DEV void tria(R* M, R* vb) {
+  Tria<R, ROWS, COLS, LD>::run(M, vb);
+}
+
+// ----------------------------------------------------------------------------- products
+
+// C = alpha op(A) op(B) (+ C when acc), C: M x N, op(A): M x K, op(B): K x N,
+// op(X) = X^T when the flag is set.
+template <typename R, int M, int K, int N, bool TA, bool TB, int LDA, int LDB, int LDC>
+SS_DEV void mm(R* C, const R* A, const R* B, R alpha = R(1), bool acc = false) {
+  constexpr int W = Vec<R>::n;
+  constexpr int KP = Pad<R, K>::n, NP = Pad<R, N>::n;
+  const int lane = lane_id();
+#pragma unroll 1
+  for (int s = 0; s < (M + 31) / 32; ++s) {
+    const int i = lane + 32 * s;
+    const int ii = i < M ? i : M - 1;
+    R a[KP];
+    if constexpr (TA) {
+      SS_UNROLL
+      for (int k = 0; k < KP; ++k) a[k] = (k < K) ? A[k * LDA + ii] : R(0);
+    } else {
+      load_row<R, K, LDA>(A, ii, a);
+    }
+    R c[NP];
+    if constexpr (!TB) {
+      SS_UNROLL
+      for (int j = 0; j < NP; ++j) c[j] = R(0);
+      SS_UNROLL
+      for (int k = 0; k < K; ++k) {
+        SS_UNROLL
+        for (int j = 0; j < NP; j += W) {
+          const Vec<R> b = ld16(B + k * LDB + j);
+          SS_UNROLL
+          for (int u = 0; u < W; ++u) c[j + u] += a[k] * b.v[u];
+        }
+      }
+    } else {
+      SS_UNROLL
+      for (int j = 0; j < NP; ++j) {
+        R t = R(0);
+        if (j < N) {
+          SS_UNROLL
+          for (int k = 0; k < KP; k += W) {
+            const Vec<R> b = ld16(B + j * LDB + k);
+            SS_UNROLL
+            for (int u = 0; u < W; ++u)
+              if (k + u < K) t += a[k + u] * b.v[u];
+          }
+        }
+        c[j] = t;
+      }
+    }
+    if (i < M) {
+      SS_UNROLL
+      for (int j = 0; j < NP; j += W) {
+        Vec<R> o;
+        if (acc) {
+          o = ld16(C + i * LDC + j);
+        } else {
+          SS_UNROLL
+          for (int u = 0; u < W; ++u) o.v[u] = R(0);
+        }
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) o.v[u] += (j + u < N) ? alpha * c[j + u] : R(0);
+        st16(C + i * LDC + j, o);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// X <- X L^{-1}, L lower triangular (N x N); the ROWS rows of X are independent.
+template <typename R, int ROWS, int N, int LDX, int LDL>
+SS_DEV void trsm_rl(R* X, const R* L) {
+  constexpr int W = Vec<R>::n, NP = Pad<R, N>::n;
+  const int lane = lane_id();
+#pragma unroll 1
+  for (int s = 0; s < (ROWS + 31) / 32; ++s) {
+    const int i = lane + 32 * s;
+    const int ii = i < ROWS ? i : ROWS - 1;
+    R x[NP];
+    load_row<R, N, LDX>(X, ii, x);
+    SS_UNROLL
+    for (int k = N - 1; k >= 0; --k) {
+      x[k] = x[k] / L[k * LDL + k];
+      SS_UNROLL
+      for (int j = 0; j < k; j += W) {
+        const Vec<R> l = ld16(L + k * LDL + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u)
+          if (j + u < k) x[j + u] -= x[k] * l.v[u];
+      }
+    }
+    __syncwarp();
+    if (i < ROWS) store_row<R, N, LDX>(X, i, x);
+  }
+  __syncwarp();
+}
+
+// X <- X L^{-T}, L lower triangular (N x N).
+template <typename R, int ROWS, int N, int LDX, int LDL>
+SS_DEV void trsm_rlt(R* X, const R* L) {
+  constexpr int W = Vec<R>::n, NP = Pad<R, N>::n;
+  const int lane = lane_id();
+#pragma unroll 1
+  for (int s = 0; s < (ROWS + 31) / 32; ++s) {
+    const int i = lane + 32 * s;
+    const int ii = i < ROWS ? i : ROWS - 1;
+    R x[NP];
+    load_row<R, N, LDX>(X, ii, x);
+    SS_UNROLL
+    for (int k = 0; k < N; ++k) {
+      R t = x[k];
+      SS_UNROLL
+      for (int j = 0; j < k; j += W) {
+        const Vec<R> l = ld16(L + k * LDL + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u)
+          if (j + u < k) t -= x[j + u] * l.v[u];
+      }
+      x[k] = t / L[k * LDL + k];
+    }
+    __syncwarp();
+    if (i < ROWS) store_row<R, N, LDX>(X, i, x);
+  }
+  __syncwarp();
+}
+
+// D (ROWS x COLS block) <- S, or <- S^T when T (S is then COLS x ROWS).
+template <typename R, int ROWS, int COLS, bool T, int LDD, int LDS>
+SS_DEV void copy(R* D, const R* S) {
+  const int lane = lane_id();
+  constexpr int CP = Pad<R, COLS>::n;
+#pragma unroll 1
+  for (int s = 0; s < (ROWS + 31) / 32; ++s) {
+    const int i = lane + 32 * s;
+    if (i < ROWS) {
+      R x[CP];
+      if constexpr (T) {
+        SS_UNROLL
+        for (int j = 0; j < CP; ++j) x[j] = (j < COLS) ? S[j * LDS + i] : R(0);
+      } else {
+        load_row<R, COLS, LDS>(S, i, x);
+      }
+      store_row<R, COLS, LDD>(D, i, x);
+    }
+  }
+  __syncwarp();
+}
+
+// D (ROWS x COLS block) <- diag * I (rows >= COLS or columns >= ROWS zero).
+template <typename R, int ROWS, int COLS, int LDD>
+SS_DEV void fill_diag(R* D, R diag) {
+  const int lane = lane_id();
+  constexpr int CP = Pad<R, COLS>::n;
+#pragma unroll 1
+  for (int s = 0; s < (ROWS + 31) / 32; ++s) {
+    const int i = lane + 32 * s;
+    if (i < ROWS) {
+      R x[CP];
+      SS_UNROLL
+      for (int j = 0; j < CP; ++j) x[j] = (j == i) ? diag : R(0);
+      store_row<R, COLS, LDD>(D, i, x);
+    }
+  }
+  __syncwarp();
+}
+
+// Lane i < M: sum_k op(A)[i][k] x[k] (x a padded shared vector).
+template <typename R, int M, int K, bool TA, int LDA>
+SS_DEV R rowdot(const R* A, const R* x, int i) {
+  constexpr int W = Vec<R>::n, KP = Pad<R, K>::n;
+  const int ii = i < M ? i : M - 1;
+  R t = R(0);
+  if constexpr (TA) {
+    SS_UNROLL
+    for (int k = 0; k < K; ++k) t += A[k * LDA + ii] * x[k];
+  } else {
+    SS_UNROLL
+    for (int k = 0; k < KP; k += W) {
+      const Vec<R> a = ld16(A + ii * LDA + k);
+      const Vec<R> b = ld16(x + k);
+      SS_UNROLL
+      for (int u = 0; u < W; ++u)
+        if (k + u < K) t += a.v[u] * b.v[u];
+    }
+  }
+  return t;
+}
+
+// Cooperative copies between a contiguous global (ROWS x COLS, row-major)
+// array and a shared matrix; COLS a multiple of the vector width, both
+// addresses 16-byte aligned.
+template <typename R, int ROWS, int COLS, int LD>
+SS_DEV void g2s(R* S, const R* G) {
+  constexpr int W = Vec<R>::n, U = COLS / W;
+  static_assert(COLS % W == 0, "columns must fill whole 16-byte units");
+  for (int q = lane_id(); q < ROWS * U; q += 32) {
+    const int r = q / U, c = (q - r * U) * W;
+    st16(S + r * LD + c, ld16(G + (size_t)r * COLS + c));
+  }
+  __syncwarp();
+}
+
+template <typename R, int ROWS, int COLS, int LD>
+SS_DEV void s2g(R* G, const R* S) {
+  constexpr int W = Vec<R>::n, U = COLS / W;
+  static_assert(COLS % W == 0, "columns must fill whole 16-byte units");
+  for (int q = lane_id(); q < ROWS * U; q += 32) {
+    const int r = q / U, c = (q - r * U) * W;
+    st16(G + (size_t)r * COLS + c, ld16(S + r * LD + c));
+  }
+  __syncwarp();
+}
+
+// Element-wise version for arrays of unknown alignment (model matrices).
+template <typename R, int ROWS, int COLS, int LD>
+SS_DEV void g2s_any(R* S, const R* G) {
+  for (int q = lane_id(); q < ROWS * COLS; q += 32) {
+    const int r = q / COLS, c = q - r * COLS;
+    S[r * LD + c] = G[q];
+  }
+  __syncwarp();
+}
+
+// Global -> global copy of n elements (16-byte aligned, n a multiple of W).
+template <typename R>
+SS_DEV void g2g(R* D, const R* S, int n) {
+  constexpr int W = Vec<R>::n;
+  for (int q = lane_id() * W; q < n; q += 32 * W) st16(D + q, ld16(S + q));
+  __syncwarp();
+}
+
+SS_DEV float warp_sum(float v) {
+  SS_UNROLL
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+SS_DEV double warp_sum(double v) {
+  SS_UNROLL
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace dense
+}  // namespace ss

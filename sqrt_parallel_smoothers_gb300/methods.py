@@ -441,11 +441,17 @@ def _lower_batched(L):
     return _lower(L).to(L.device).contiguous()
 
 
-def _dummy_observation(nx, dtype, device):
+def _dummy_observation(nx, dtype, device, ny=1):
     from .models import LinearModel
-    fn = LinearModel(torch.zeros(1, nx))
-    return fn, _as(fn.A, dtype, device), torch.zeros(1, dtype=dtype, device=device), \
-        torch.ones(1, 1, dtype=dtype, device=device)
+    fn = LinearModel(torch.zeros(ny, nx))
+    return fn, _as(fn.A, dtype, device), torch.zeros(ny, dtype=dtype, device=device), \
+        torch.eye(ny, dtype=dtype, device=device)
+
+
+def _dummy_ny(nx):
+    """Observation size of the placeholder model when a transition is linearised alone: the
+    compiled large-state (nx > 5) kernels pair nx with ny = nx / 2."""
+    return 1 if nx <= 5 else nx // 2
 
 
 def filtering(observations, x0, transition_model, observation_model, linearization_method,
@@ -498,11 +504,12 @@ def smoothing(transition_model, filter_trajectory, linearization_method, nominal
         B, Tp1 = fm.shape[:2]
         lay = _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
     fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
-    fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev)
+    ny = _dummy_ny(nx)
+    fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev, ny)
     fmp = lay.pack_states(filter_trajectory.mean, (nx,))
     fLp = _lower_batched(lay.pack_states(filter_trajectory.chol, (nx, nx)))
     nm, nL = _nominal(nominal_trajectory, lay, nx)
-    icfg = _icfg(method, nx, 1, fn_t, fn_o, lay, chunk, group, slr_form, [0, 0])
+    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, [0, 0])
     out_m, out_L = torch.ops.sqrtsmooth.smooth(fmp, fLp, lay.offsets, nm, nL, t_mat, t_qm, t_qL, o_mat, o_qm,
                                                o_qL, icfg, _fcfg(method, fn_t, fn_o))
     return MVNSqrt(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_L, (nx, nx)))
@@ -578,8 +585,8 @@ def linearize(model, x, method):
         ny = d_out
     else:
         fn_t, t_mat, t_qm, t_qL = fnm, mat, qm, qL
-        o = _dummy_observation(nx, dtype, dev)
-        ny = 1
+        ny = _dummy_ny(nx)
+        o = _dummy_observation(nx, dtype, dev, ny)
     lay_off = torch.zeros(2, dtype=torch.int64, device=dev)
 
     class _L:

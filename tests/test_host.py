@@ -76,6 +76,28 @@ def test_workspace_query_and_validation():
     assert lib.ss_supported(ctypes.byref(p4)) == 1
 
 
+def test_large_state_dims_are_linear_only():
+    """The large-state kernels (nx = 8 and 32) take linear models only; their workspace
+    holds one smoothing element per step, which dominates at the large-state workload."""
+    lib = _lib.load()
+    n = ctypes.c_size_t(0)
+    for nx, ny in ((8, 4), (32, 16)):
+        for dt in (_lib.SS_F32, _lib.SS_F64):
+            p, keep = _problem(nx=nx, ny=ny, dtype=dt)
+            assert lib.ss_supported(ctypes.byref(p)) == 1
+            assert lib.ss_workspace_bytes(ctypes.byref(p), ctypes.byref(n)) == 0
+            assert n.value > 0
+            p.transition.kind = _lib.SS_MODEL_COORDINATED_TURN
+            assert lib.ss_supported(ctypes.byref(p)) == 0
+    p, keep = _problem(nx=32, ny=16, batch=16)
+    p.total_steps, p.max_len = 16 * 131072, 131072
+    assert lib.ss_workspace_bytes(ctypes.byref(p), ctypes.byref(n)) == 0
+    per_step = (2 * 32 * 32 + 32) * 4
+    assert per_step * p.total_steps <= n.value <= 4 * per_step * p.total_steps
+    p2, keep2 = _problem(nx=16, ny=8)
+    assert lib.ss_supported(ctypes.byref(p2)) == 0
+
+
 def test_calls_without_workspace_fail_cleanly():
     lib = _lib.load()
     p, keep = _problem()
