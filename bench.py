@@ -286,6 +286,135 @@ def adjoint_section(torch, S, flush):
             "max_rel_err": float(np.max(rel)), "method": "tangent-linear filter, one pass per parameter"}
 
 
+def cv_section(torch, S, flush):
+    """Constant-velocity linear model (nx = 4, ny = 2, dt = 0.1, q = 0.1, R = 0.5 I, m0 = 0,
+    P0 = I), T = 1000 from seed 0, FP64: one parallel square-root filter + RTS smoother pass
+    (the smoother at a given nominal, replayed as a CUDA graph).  Its agreement with the FP64
+    oracle (1e-10) is checked in the GPU tests."""
+    w = S.data.cv_workload(1000, seed=0)
+    d = torch.float64
+    tm = S.FunctionalModel(S.models.LinearModel(torch.as_tensor(w["F"])),
+                           S.MVNSqrt(torch.zeros(4, dtype=d), torch.as_tensor(np.linalg.cholesky(w["Q"]))))
+    om = S.FunctionalModel(S.models.LinearModel(torch.as_tensor(w["H"])),
+                           S.MVNSqrt(torch.zeros(2, dtype=d), torch.as_tensor(np.linalg.cholesky(w["R"]))))
+    x0 = S.MVNSqrt(torch.zeros(4, dtype=d), torch.eye(4, dtype=d))
+    nom = S.MVNSqrt(torch.zeros(1001, 4, dtype=d), torch.eye(4, dtype=d).expand(1001, 4, 4).contiguous())
+    plan = S.IteratedSmootherPlan(torch.as_tensor(w["ys"], dtype=d), x0, tm, om, S.linearization.extended, nom,
+                                  criterion=S.FixedIterations(1), graph=True)
+    ms, _ = time_plan(torch, plan, 10, 3, flush)
+    return {"workload": "constant velocity nx=4 ny=2, T=1000, FP64, one filter+smoother pass",
+            "ms": float(np.median(ms)), "timesteps_per_s": 1000 / (float(np.median(ms)) * 1e-3)}
+
+
+def sweep_section(torch, S, flush):
+    """Single-sequence bearings smoother (10 calls from the prior mean broadcast) for
+    T = 1e2 .. 1e5, FP64 then FP32: timesteps/s and the FP32 position RMSE against FP64's."""
+    out = []
+    for k, T in enumerate((100, 1000, 10_000, 100_000)):
+        one = S.data.bearings_batch(np.array([T]), qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=30_000 + k)
+        row = {"T": T}
+        means = {}
+        for name, dt in (("fp64", torch.float64), ("fp32", torch.float32)):
+            plan = make_plan(torch, S, one["ys"], one["offsets"], dt)
+            ms, _ = time_plan(torch, plan, 3, 3, flush)
+            row[name] = {"ms": float(np.median(ms)), "timesteps_per_s": T / (float(np.median(ms)) * 1e-3)}
+            means[name] = plan.mean.double().cpu().numpy()
+            del plan
+        xs = one["xs"].astype(np.float64)
+        r64 = position_rmse(means["fp64"], xs, one["offsets"])[0]
+        r32 = position_rmse(means["fp32"], xs, one["offsets"])[0]
+        row["rmse_fp64"], row["rmse_fp32"] = float(r64), float(r32)
+        row["rmse_rel_diff"] = float(abs(r32 - r64) / max(r64, 1e-12))
+        out.append(row)
+        torch.cuda.empty_cache()
+    return out
+
+
+# Algorithmic FP32 flops per step of the large-state kernels (nx = 32, ny = 16): a Householder
+# lower-triangularisation of an r x c matrix costs 4 sum_{p<r} (c - p)(r - p) flops.
+def _tria_flops(r, c):
+    return 4 * sum((c - p) * (r - p) for p in range(r))
+
+
+LARGE_FLOPS_PER_STEP = {
+    "filter_walk": _tria_flops(64, 64) + _tria_flops(48, 48) + 32 ** 3 + 16 * 32 ** 2 + 32 ** 3 + 6 * 32 * 32,
+    "smoother_leaf": _tria_flops(32, 64) + 2 * 32 ** 3 + 32 ** 3 + 2 * 32 * 32,
+    "smoother_walk": _tria_flops(32, 64) + 32 ** 3 + 2 * 32 * 32,
+}
+
+
+def large_state_section(torch, S, flush, chunk=32):
+    """The large-state regime: random stable linear SSM nx = 32, ny = 16, B = 16 sequences of
+    T = 131 072, FP32, 10 filter-smoother passes (the default-nominal pass and 9 counted calls;
+    a linear model's passes are identical), one CUDA graph.  Errors of the smoothed means and
+    covariances against the FP64 path (itself pinned to the FP64 oracle in the tests)."""
+    from sqrt_parallel_smoothers_gb300 import _lib
+    B, T, nx, ny = 16, 131_072, 32, 16
+    F, Q, H, R = S.data.large_state_model(nx, ny, 0)
+    rng = np.random.RandomState(1)
+    cQ, cR = np.linalg.cholesky(Q), np.linalg.cholesky(R)
+    x = rng.randn(B, nx)
+    ys = np.zeros((B, T, ny), np.float32)
+    for t in range(T):
+        x = x @ F.T + rng.randn(B, nx) @ cQ.T
+        ys[:, t] = x @ H.T + rng.randn(B, ny) @ cR.T
+    offsets = np.arange(B + 1) * T
+
+    def setup(dt):
+        tm = S.FunctionalModel(S.models.LinearModel(torch.as_tensor(F, dtype=dt)),
+                               S.MVNSqrt(torch.zeros(nx, dtype=dt), torch.as_tensor(cQ, dtype=dt)))
+        om = S.FunctionalModel(S.models.LinearModel(torch.as_tensor(H, dtype=dt)),
+                               S.MVNSqrt(torch.zeros(ny, dtype=dt), torch.as_tensor(cR, dtype=dt)))
+        return tm, om, S.MVNSqrt(torch.zeros(nx, dtype=dt), torch.eye(nx, dtype=dt))
+
+    tm, om, x0 = setup(torch.float32)
+    y32 = torch.as_tensor(ys.reshape(-1, ny))
+    plan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None, criterion=S.FixedIterations(9),
+                                  offsets=offsets, chunk=chunk, group=8, graph=True)
+    ms, _ = time_plan(torch, plan, 2, 1, flush)
+    step_ms = float(np.median(ms))
+    m32 = plan.mean.double().cpu()
+    L32 = plan.chol.cpu()
+    launches = plan.launches_per_run
+    del plan
+    torch.cuda.empty_cache()
+    pplan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None, criterion=S.FixedIterations(9),
+                                   offsets=offsets, chunk=chunk, group=8, graph=True, profile=True)
+    pplan.run()
+    torch.cuda.synchronize()
+    prof = _lib.profile_read()
+    del pplan
+    _lib.profile_reset()
+    torch.cuda.empty_cache()
+    tot = sum(v[1] for v in prof.values()) or 1.0
+    kern = {k: {"launches": v[0], "total_ms": v[1], "share": v[1] / tot} for k, v in prof.items()}
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    roof = None
+    if dom in LARGE_FLOPS_PER_STEP:
+        per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
+        ach = LARGE_FLOPS_PER_STEP[dom] * B * T / (per_launch_ms * 1e-3) / 1e12
+        roof = {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": 80.5, "unit": "TFLOP/s", "frac": ach / 80.5,
+                "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); no measured FP32 peak",
+                "alg_flops_per_step": LARGE_FLOPS_PER_STEP[dom]}
+    tm64, om64, x064 = setup(torch.float64)
+    res64 = S.iterated_smoothing(torch.as_tensor(ys.reshape(-1, ny), dtype=torch.float64), x064, tm64, om64,
+                                 S.linearization.cubature, None, criterion=S.FixedIterations(1), offsets=offsets,
+                                 chunk=chunk)
+    m64 = res64.mean.cpu()
+    idx = torch.arange(0, m64.shape[0], 97)
+    L64 = res64.chol[idx.to(res64.chol.device)].cpu()
+    del res64
+    torch.cuda.empty_cache()
+    C32 = L32[idx].double() @ L32[idx].double().transpose(-1, -2)
+    C64 = L64 @ L64.transpose(-1, -2)
+    return {"workload": "linear nx=32 ny=16 (F = 0.98 Haar, Q = L L^T/nx, H ~ N(0, 1/nx), R = 0.1 I), B=16, "
+                        "T=131072, FP32, 10 filter-smoother passes, chunk 32, one CUDA graph",
+            "ms_per_step": step_ms, "timesteps_per_s": B * T / (step_ms * 1e-3), "gpu_launches": launches,
+            "mean_err_rel_vs_fp64": float((m32 - m64).abs().max() / m64.abs().max()),
+            "cov_err_rel_vs_fp64": float((C32 - C64).abs().max() / C64.abs().max()),
+            "kernels": kern, "roofline": roof}
+
+
 def gpu_arm(args):
     import torch
     import sqrt_parallel_smoothers_gb300 as S
@@ -436,6 +565,10 @@ def gpu_arm(args):
                         "rmse": "position RMSE of smoothed means vs simulated truth, per sequence"}
 
     line["adjoint"] = adjoint_section(torch, S, flush)
+    if not args.no_extra:
+        line["cv_fp64"] = cv_section(torch, S, flush)
+        line["sweep_T"] = sweep_section(torch, S, flush)
+        line["large_state"] = large_state_section(torch, S, flush)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         seqs, tot = cpu_sample(lengths, batch, budget_steps=6000)
@@ -462,6 +595,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-main", action="store_true", help="time the FP32 batched smoother only")
     ap.add_argument("--no-autotune", action="store_true", help="use the default chunk/group (16, 8)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the T sweep and the large-state workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

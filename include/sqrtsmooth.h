@@ -72,6 +72,12 @@ typedef struct ss_model {
   const void* noise_chol;  /* (d_out, d_out) lower triangular, device */
 } ss_model;
 
+/* ss_problem.options bits.  For linear models with nx > 5, a batch of equally long
+ * sequences that share one prior has one covariance recursion: the large-state path then
+ * computes every factor once and only the means per sequence (up to 32 sequences).  This
+ * bit forces the per-sequence computation instead. */
+#define SS_OPT_PER_SEQUENCE_COVARIANCE 1
+
 typedef struct ss_problem {
   int32_t dtype;           /* SS_F32 or SS_F64 */
   int32_t nx, ny;
@@ -82,7 +88,7 @@ typedef struct ss_problem {
   int32_t slr_form;        /* SS_SLR_AUTO, 1 or 2 */
   int32_t chunk;           /* steps per level-0 chunk, 0 = default */
   int32_t group;           /* summaries per group at higher scan levels, 0 = default */
-  int32_t reserved;
+  int32_t options;         /* SS_OPT_* bits, 0 = defaults */
   ss_model transition;     /* nx -> nx */
   ss_model observation;    /* nx -> ny */
   int64_t batch;           /* B >= 1 */

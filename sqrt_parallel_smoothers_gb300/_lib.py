@@ -15,6 +15,7 @@ SS_LIN_EXTENDED, SS_LIN_CUBATURE, SS_LIN_UNSCENTED, SS_LIN_GAUSS_HERMITE = 0, 1,
 SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS = 0, 1, 2
 SS_MAX_GH_ORDER = 8
 SS_MAX_TANGENTS = 4
+SS_OPT_PER_SEQUENCE_COVARIANCE = 1
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
             "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",
@@ -32,7 +33,7 @@ class SSProblem(ctypes.Structure):
                 ("lin_method", ctypes.c_int32), ("ut_alpha", ctypes.c_double), ("ut_beta", ctypes.c_double),
                 ("ut_kappa", ctypes.c_double), ("ut_kappa_default", ctypes.c_int32),
                 ("gh_order", ctypes.c_int32), ("slr_form", ctypes.c_int32), ("chunk", ctypes.c_int32),
-                ("group", ctypes.c_int32), ("reserved", ctypes.c_int32), ("transition", SSModel),
+                ("group", ctypes.c_int32), ("options", ctypes.c_int32), ("transition", SSModel),
                 ("observation", SSModel), ("batch", ctypes.c_int64), ("total_steps", ctypes.c_int64),
                 ("max_len", ctypes.c_int64), ("offsets", ctypes.c_void_p)]
 

@@ -105,10 +105,16 @@ SS_DEV void store_row(R* M, int r, const R (&x)[Pad<R, COLS>::n]) {
 // M <- [L 0] = M Q, Q orthogonal, L lower triangular with a non-negative
 // diagonal: Householder reflections from the right (Golub & Van Loan,
 // Algorithm 5.1.1, with Parlett's formula for the sign-free reflector, so the
-// diagonal comes out non-negative without a second pass).  The pivot lane
-// publishes each reflector in vb (>= Pad<COLS>::n + W elements, 16-byte
-// aligned); pivots are processed in blocks of eight so that every register
-// index stays compile-time.
+// diagonal comes out non-negative without a second pass).
+//
+// Per pivot p the pivot lane publishes its row in one of two alternating
+// buffers (so one warp barrier per pivot suffices), every lane sums two of the
+// squared entries and a butterfly gives all lanes the norm, and each lane
+// applies the reflector to its rows with split accumulators.  The published
+// row keeps x_p; the reflector's v_p differs from it only at p, which is
+// corrected with one select over the eight pivots of the block.  Pivots are
+// processed in blocks of eight so that every register index is compile-time.
+// vb holds two buffers of Pad<COLS>::n elements each (16-byte aligned).
 template <typename R, int ROWS, int COLS, int LD>
 struct Tria {
   static constexpr int W = Vec<R>::n;
@@ -121,25 +127,38 @@ struct Tria {
   static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
     const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
     for (int p = J0; p < pend; ++p) {
+      R* v = vb + (p & 1) * CP;
+      const int ps = p >> 5;
       if (lane == (p & 31)) {
-        const int ps = p >> 5;
-        R x0 = R(0), sig = R(0);
         SS_UNROLL
         for (int j = J0; j < CP; ++j) {
           R xj = row[0][j];
           if constexpr (NS > 1) {
             if (ps == 1) xj = row[1][j];
           }
-          if (j == p) x0 = xj;
-          const R vj = (j > p && j < COLS) ? xj : R(0);
-          sig += vj * vj;
-          vb[j] = vj;
+          v[j] = (j >= p && j < COLS) ? xj : R(0);
         }
-        const R nrm = ss_sqrt(x0 * x0 + sig);
-        const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
-        const R vv = v0 * v0 + sig;
-        vb[p] = v0;
-        vb[CP] = (vv > R(0)) ? R(2) / vv : R(0);
+      }
+      __syncwarp();
+      R part = R(0);
+      SS_UNROLL
+      for (int q = 0; q < CP - J0; q += 32) {
+        const int j = J0 + q + lane;
+        if (j < CP && j > p) {
+          const R x = v[j];
+          part += x * x;
+        }
+      }
+      SS_UNROLL
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const R sig = part;
+      const R x0 = v[p];
+      const R nrm = ss_sqrt(x0 * x0 + sig);
+      const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
+      const R vv = v0 * v0 + sig;
+      const R tau = (vv > R(0)) ? R(2) / vv : R(0);
+      const R dv = v0 - x0;   // v_p - x_p
+      if (lane == (p & 31)) {
         SS_UNROLL
         for (int s = 0; s < NS; ++s) {
           if (s == ps) {
@@ -151,35 +170,50 @@ struct Tria {
           }
         }
       }
-      __syncwarp();
-      const R tau = vb[CP];
-      R d[NS];
+      R d0[NS], d1[NS], rp[NS];
       SS_UNROLL
-      for (int s = 0; s < NS; ++s) d[s] = R(0);
+      for (int s = 0; s < NS; ++s) {
+        d0[s] = R(0);
+        d1[s] = R(0);
+        rp[s] = R(0);
+        SS_UNROLL
+        for (int j = J0; j < J0 + 8 && j < CP; ++j)
+          if (j == p) rp[s] = row[s][j];
+      }
       SS_UNROLL
       for (int j = J0; j < CP; j += W) {
-        const Vec<R> v = ld16(vb + j);
+        const Vec<R> x = ld16(v + j);
         SS_UNROLL
         for (int u = 0; u < W; ++u) {
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) d[s] += row[s][j + u] * v.v[u];
+          for (int s = 0; s < NS; ++s) {
+            if (u & 1) d1[s] += row[s][j + u] * x.v[u];
+            else d0[s] += row[s][j + u] * x.v[u];
+          }
+        }
+      }
+      R f[NS];
+      SS_UNROLL
+      for (int s = 0; s < NS; ++s) {
+        const int r = lane + 32 * s;
+        const R d = d0[s] + d1[s] + rp[s] * dv;
+        f[s] = (r > p && r < ROWS) ? tau * d : R(0);
+      }
+      SS_UNROLL
+      for (int j = J0; j < CP; j += W) {
+        const Vec<R> x = ld16(v + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) {
+          SS_UNROLL
+          for (int s = 0; s < NS; ++s) row[s][j + u] -= f[s] * x.v[u];
         }
       }
       SS_UNROLL
       for (int s = 0; s < NS; ++s) {
-        const int r = lane + 32 * s;
-        d[s] = (r > p && r < ROWS) ? tau * d[s] : R(0);
-      }
-      SS_UNROLL
-      for (int j = J0; j < CP; j += W) {
-        const Vec<R> v = ld16(vb + j);
         SS_UNROLL
-        for (int u = 0; u < W; ++u) {
-          SS_UNROLL
-          for (int s = 0; s < NS; ++s) row[s][j + u] -= d[s] * v.v[u];
-        }
+        for (int j = J0; j < J0 + 8 && j < CP; ++j)
+          if (j == p) row[s][j] -= f[s] * dv;
       }
-      __syncwarp();
     }
   }
 
@@ -211,6 +245,10 @@ struct Tria {
   }
 };
 
+// Scratch elements tria<., COLS> needs for its reflector buffers.
+template <typename R, int COLS>
+__host__ __device__ constexpr int tria_scratch() { return 2 * Pad<R, COLS>::n; }
+
 template <typename R, int ROWS, int COLS, int LD>
 SS_DEV void tria(R* M, R* vb) {
   Tria<R, ROWS, COLS, LD>::run(M, vb);
@@ -220,7 +258,8 @@ SS_DEV void tria(R* M, R* vb) {
 
 // C = alpha op(A) op(B) (+ C when acc), C: M x N, op(A): M x K, op(B): K x N,
 // op(X) = X^T when the flag is set.
-template <typename R, int M, int K, int N, bool TA, bool TB, int LDA, int LDB, int LDC>
+// LB: B is lower triangular (its strict upper part is skipped).
+template <typename R, int M, int K, int N, bool TA, bool TB, int LDA, int LDB, int LDC, bool LB = false>
 SS_DEV void mm(R* C, const R* A, const R* B, R alpha = R(1), bool acc = false) {
   constexpr int W = Vec<R>::n;
   constexpr int KP = Pad<R, K>::n, NP = Pad<R, N>::n;
@@ -244,6 +283,7 @@ SS_DEV void mm(R* C, const R* A, const R* B, R alpha = R(1), bool acc = false) {
       for (int k = 0; k < K; ++k) {
         SS_UNROLL
         for (int j = 0; j < NP; j += W) {
+          if (LB && j > k) continue;
           const Vec<R> b = ld16(B + k * LDB + j);
           SS_UNROLL
           for (int u = 0; u < W; ++u) c[j + u] += a[k] * b.v[u];

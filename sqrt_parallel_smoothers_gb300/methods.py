@@ -235,9 +235,20 @@ def _ptr(t):
     return None if t is None else t.data_ptr()
 
 
+_OPTIONS = {"per_sequence_covariance": False}
+
+
+def set_large_state_options(per_sequence_covariance=False):
+    """Large-state path (linear models, nx > 5): by default a batch of equally long sequences
+    with one shared prior computes its common covariance recursion once and the means per
+    sequence; ``per_sequence_covariance=True`` computes every sequence separately."""
+    _OPTIONS["per_sequence_covariance"] = bool(per_sequence_covariance)
+
+
 def _problem(icfg, fcfg, dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL):
     (nx, ny, code, kdef, order, slr, chunk, group, tk, ok, B, N, maxlen) = icfg[:13]
     pr = _lib.SSProblem()
+    pr.options = _lib.SS_OPT_PER_SEQUENCE_COVARIANCE if _OPTIONS["per_sequence_covariance"] else 0
     pr.dtype = _DT[dtype]
     pr.nx, pr.ny, pr.lin_method = nx, ny, code
     pr.ut_alpha, pr.ut_beta, pr.ut_kappa = fcfg[0], fcfg[1], fcfg[2]

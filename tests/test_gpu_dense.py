@@ -135,3 +135,61 @@ def test_dense_large_workload_fp32_tracks_fp64():
     assert float(torch.triu(a.chol, 1).abs().max()) == 0.0
     assert_rel(a.mean, b.mean, 1e-3, "fp32 vs fp64 means")
     assert_rel(cov(a.chol), cov(b.chol), 1e-3, "fp32 vs fp64 covariances")
+
+
+@pytest.fixture
+def per_sequence_covariance():
+    S.set_large_state_options(per_sequence_covariance=True)
+    yield
+    S.set_large_state_options(per_sequence_covariance=False)
+
+
+def _equal_batch(nx, ny, B=3, T=45, seed=9):
+    sysm, (ot, oo), (gt, go) = _system(nx, ny, seed=seed)
+    lengths = np.full(B, T)
+    ys = _observations(sysm, lengths, seed=seed)
+    m0, L0 = _prior(nx)
+    return lengths, ys, m0, L0, (ot, oo), (gt, go)
+
+
+@pytest.mark.parametrize("nx,ny", DIMS)
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-9), (torch.float32, 2e-3)])
+def test_dense_shared_covariance_vs_oracle(nx, ny, dtype, tol):
+    """Equally long sequences with one prior: the factor recursion is computed once for the
+    batch (shared-covariance mode); every sequence still matches the oracle."""
+    lengths, ys, m0, L0, (ot, oo), (gt, go) = _equal_batch(nx, ny)
+    x0 = S.MVNSqrt(torch.as_tensor(m0), torch.as_tensor(L0))
+    filt, ell = S.filtering(torch.as_tensor(ys, dtype=dtype), x0, gt, go, S.linearization.extended, None,
+                            return_loglikelihood=True, lengths=lengths, chunk=8, group=2)
+    res, ell2, info = S.iterated_smoothing(torch.as_tensor(ys, dtype=dtype), x0, gt, go, S.linearization.cubature,
+                                           None, criterion=lambda i, *_: i < 2, return_loglikelihood=True,
+                                           lengths=lengths, return_info=True, chunk=8, group=2)
+    for i, T in enumerate(lengths):
+        ref_f, ref_ell = O.methods.filtering(ys[i], O.MVNSqrt(m0, L0), ot, oo, O.linearization.extended, None, True,
+                                             return_loglikelihood=True)
+        assert_rel(filt.mean[i], ref_f.mean, tol, f"seq {i} filtered mean")
+        assert_rel(cov(filt.chol[i]), cov(ref_f.chol), tol, f"seq {i} filtered cov")
+        assert abs(float(ell[i]) - ref_ell) <= tol * abs(ref_ell)
+        ref_s = O.methods.smoothing(ot, ref_f, O.linearization.extended, None, True)
+        assert_rel(res.mean[i], ref_s.mean, tol, f"seq {i} smoothed mean")
+        assert_rel(cov(res.chol[i]), cov(ref_s.chol), tol, f"seq {i} smoothed cov")
+        assert abs(float(ell2[i]) - ref_ell) <= tol * abs(ref_ell)
+    assert int(info["flags"].abs().sum()) == 0
+
+
+@pytest.mark.parametrize("nx,ny", DIMS)
+def test_dense_shared_equals_per_sequence(nx, ny, per_sequence_covariance):
+    """Shared-covariance and per-sequence computation agree to rounding (FP64), including the
+    tolerance criterion that stops sequences on their own."""
+    lengths, ys, m0, L0, _, (gt, go) = _equal_batch(nx, ny, B=5, T=64, seed=4)
+    x0 = S.MVNSqrt(torch.as_tensor(m0), torch.as_tensor(L0))
+    out = {}
+    for per_seq in (True, False):
+        S.set_large_state_options(per_sequence_covariance=per_seq)
+        res, info = S.iterated_smoothing(torch.as_tensor(ys), x0, gt, go, S.linearization.extended, None,
+                                         lengths=lengths, return_info=True, chunk=8, group=2)
+        out[per_seq] = (res, info)
+    a, b = out[True][0], out[False][0]
+    assert_rel(a.mean, b.mean, 1e-11, "means")
+    assert_rel(cov(a.chol), cov(b.chol), 1e-11, "covariances")
+    assert torch.equal(out[True][1]["iterations"], out[False][1]["iterations"])
