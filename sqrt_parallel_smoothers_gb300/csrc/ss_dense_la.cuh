@@ -100,6 +100,20 @@ SS_DEV void store_row(R* M, int r, const R (&x)[Pad<R, COLS>::n]) {
   }
 }
 
+// Columns [OFF, OFF + N) of a register row into row r of a shared matrix.
+template <typename R, int N, int LD, int OFF, int CPX>
+SS_DEV void store_part(R* M, int r, const R (&x)[CPX]) {
+  constexpr int W = Vec<R>::n;
+  static_assert(OFF + Pad<R, N>::n <= CPX, "part outside the row");
+  SS_UNROLL
+  for (int j = 0; j < Pad<R, N>::n; j += W) {
+    Vec<R> v;
+    SS_UNROLL
+    for (int u = 0; u < W; ++u) v.v[u] = (j + u < N) ? x[OFF + j + u] : R(0);
+    st16(M + r * LD + j, v);
+  }
+}
+
 // ----------------------------------------------------------------------------- tria
 
 // M <- [L 0] = M Q, Q orthogonal, L lower triangular with a non-negative
@@ -107,19 +121,21 @@ SS_DEV void store_row(R* M, int r, const R (&x)[Pad<R, COLS>::n]) {
 // Algorithm 5.1.1, with Parlett's formula for the sign-free reflector, so the
 // diagonal comes out non-negative without a second pass).
 //
-// Per pivot p the pivot lane publishes its row in one of two alternating
-// buffers (so one warp barrier per pivot suffices), every lane sums two of the
-// squared entries and a butterfly gives all lanes the norm, and each lane
-// applies the reflector to its rows with split accumulators.  The published
-// row keeps x_p; the reflector's v_p differs from it only at p, which is
-// corrected with one select over the eight pivots of the block.  Pivots are
-// processed in blocks of eight so that every register index is compile-time.
-// vb holds two buffers of Pad<COLS>::n elements each (16-byte aligned).
+// Per pivot p the pivot lane publishes its row (16-byte stores) and the
+// squared norm of its part right of p (four partial sums) in one of two
+// alternating buffers, so one warp barrier per pivot suffices; each lane then
+// applies the reflector to its one or two rows with split accumulators.  The
+// published row keeps x_p; the reflector's v_p differs from it only at p,
+// which is corrected with one select over the eight pivots of the block.
+// Pivots are processed in blocks of eight so that every register index is
+// compile-time.  vb holds two buffers of Pad<COLS>::n + W elements (16-byte
+// aligned): tria_scratch().
 template <typename R, int ROWS, int COLS, int LD>
 struct Tria {
   static constexpr int W = Vec<R>::n;
   static constexpr int CP = Pad<R, COLS>::n;
   static constexpr int NS = (ROWS + 31) / 32;
+  static constexpr int VS = CP + W;   // one reflector buffer
   static_assert(ROWS <= COLS, "tria needs rows <= cols");
   static_assert(LD >= CP, "row stride too small");
 
@@ -127,31 +143,31 @@ struct Tria {
   static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
     const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
     for (int p = J0; p < pend; ++p) {
-      R* v = vb + (p & 1) * CP;
+      R* v = vb + (p & 1) * VS;
       const int ps = p >> 5;
       if (lane == (p & 31)) {
+        R sq[4] = {R(0), R(0), R(0), R(0)};
         SS_UNROLL
-        for (int j = J0; j < CP; ++j) {
-          R xj = row[0][j];
-          if constexpr (NS > 1) {
-            if (ps == 1) xj = row[1][j];
+        for (int j = J0; j < CP; j += W) {
+          Vec<R> o;
+          SS_UNROLL
+          for (int u = 0; u < W; ++u) {
+            const int jj = j + u;
+            R xj = row[0][jj];
+            if constexpr (NS > 1) {
+              if (ps == 1) xj = row[1][jj];
+            }
+            const R m = (jj >= p && jj < COLS) ? xj : R(0);
+            o.v[u] = m;
+            const R q = (jj > p) ? m : R(0);
+            sq[jj & 3] += q * q;
           }
-          v[j] = (j >= p && j < COLS) ? xj : R(0);
+          st16(v + j, o);
         }
+        v[CP] = (sq[0] + sq[1]) + (sq[2] + sq[3]);
       }
       __syncwarp();
-      R part = R(0);
-      SS_UNROLL
-      for (int q = 0; q < CP - J0; q += 32) {
-        const int j = J0 + q + lane;
-        if (j < CP && j > p) {
-          const R x = v[j];
-          part += x * x;
-        }
-      }
-      SS_UNROLL
-      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-      const R sig = part;
+      const R sig = v[CP];
       const R x0 = v[p];
       const R nrm = ss_sqrt(x0 * x0 + sig);
       const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
@@ -170,11 +186,11 @@ struct Tria {
           }
         }
       }
-      R d0[NS], d1[NS], rp[NS];
+      R d[NS][4], rp[NS];
       SS_UNROLL
       for (int s = 0; s < NS; ++s) {
-        d0[s] = R(0);
-        d1[s] = R(0);
+        SS_UNROLL
+        for (int k = 0; k < 4; ++k) d[s][k] = R(0);
         rp[s] = R(0);
         SS_UNROLL
         for (int j = J0; j < J0 + 8 && j < CP; ++j)
@@ -186,18 +202,15 @@ struct Tria {
         SS_UNROLL
         for (int u = 0; u < W; ++u) {
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) {
-            if (u & 1) d1[s] += row[s][j + u] * x.v[u];
-            else d0[s] += row[s][j + u] * x.v[u];
-          }
+          for (int s = 0; s < NS; ++s) d[s][(j + u) & 3] += row[s][j + u] * x.v[u];
         }
       }
       R f[NS];
       SS_UNROLL
       for (int s = 0; s < NS; ++s) {
         const int r = lane + 32 * s;
-        const R d = d0[s] + d1[s] + rp[s] * dv;
-        f[s] = (r > p && r < ROWS) ? tau * d : R(0);
+        const R dd = (d[s][0] + d[s][1]) + (d[s][2] + d[s][3]) + rp[s] * dv;
+        f[s] = (r > p && r < ROWS) ? tau * dd : R(0);
       }
       SS_UNROLL
       for (int j = J0; j < CP; j += W) {
@@ -220,6 +233,13 @@ struct Tria {
   template <int... B>
   static SS_DEV void blocks(R (&row)[NS][CP], R* vb, int lane, std::integer_sequence<int, B...>) {
     (block<8 * B>(row, vb, lane), ...);
+  }
+
+  // The rows already in registers (row r = lane r % 32, slot r / 32; rows >= ROWS and
+  // columns >= COLS zero).
+  static SS_DEV void run_regs(R (&row)[NS][CP], R* vb) {
+    blocks(row, vb, lane_id(), std::make_integer_sequence<int, (ROWS + 7) / 8>{});
+    __syncwarp();
   }
 
   static SS_DEV void run(R* M, R* vb) {
@@ -247,7 +267,7 @@ struct Tria {
 
 // Scratch elements tria<., COLS> needs for its reflector buffers.
 template <typename R, int COLS>
-__host__ __device__ constexpr int tria_scratch() { return 2 * Pad<R, COLS>::n; }
+__host__ __device__ constexpr int tria_scratch() { return 2 * (Pad<R, COLS>::n + Vec<R>::n); }
 
 template <typename R, int ROWS, int COLS, int LD>
 SS_DEV void tria(R* M, R* vb) {

@@ -338,7 +338,7 @@ template <typename R, int NX, int NY>
 __host__ __device__ constexpr int walk_b_warp_elems() {
   typedef DS<R, NX, NY> S;
   typedef DSS<R, NX, NY> SS;
-  return S::MN + S::MPHI + 3 * SS::MB + 2 * SS::MBY + S::VB;
+  return 2 * S::MN + (NY + NX) * S::LDY + 3 * SS::MB + 2 * SS::MBY + S::VB;
 }
 template <typename R, int NX, int NY>
 __host__ __device__ constexpr int walk_b_warps() {
@@ -351,8 +351,91 @@ __host__ __device__ constexpr int walk_b_elems() {
   return mc_elems<R, NX, NY>() + walk_b_warps<R, NX, NY>() * walk_b_warp_elems<R, NX, NY>();
 }
 
+// Row r of Phi = [[F L, cQ], [L, 0]] (L lower, in shared memory) into registers,
+// row r in lane r % 32, slot r / 32.
+template <typename R, int NX, int NY>
+SS_DEV void phi_rows(MC<R> c, const R* L, R (&row)[(2 * NX + 31) / 32][Pad<R, 2 * NX>::n]) {
+  typedef DS<R, NX, NY> S;
+  constexpr int W = S::W, CP = Pad<R, 2 * NX>::n;
+  const int l = lane_id();
+  SS_UNROLL
+  for (int s = 0; s < (2 * NX + 31) / 32; ++s) {
+    const int r = l + 32 * s;
+    SS_UNROLL
+    for (int j = 0; j < CP; ++j) row[s][j] = R(0);
+    if (r < NX) {
+      R f[S::VN];
+      load_row<R, NX, S::LDN>(c.F, r, f);
+      SS_UNROLL
+      for (int k = 0; k < NX; ++k) {
+        SS_UNROLL
+        for (int j = 0; j <= k; j += W) {
+          const Vec<R> b = ld16(L + k * S::LDN + j);
+          SS_UNROLL
+          for (int u = 0; u < W; ++u) row[s][j + u] += f[k] * b.v[u];
+        }
+      }
+      SS_UNROLL
+      for (int j = 0; j < NX; j += W) {
+        const Vec<R> q = ld16(c.cQ + r * S::LDN + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) row[s][NX + j + u] = q.v[u];
+      }
+    } else if (r < 2 * NX) {
+      SS_UNROLL
+      for (int j = 0; j < NX; j += W) {
+        const Vec<R> q = ld16(L + (r - NX) * S::LDN + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) row[s][j + u] = q.v[u];
+      }
+    }
+  }
+}
+
+// Row r of Psi = [[H N1, cR], [N1, 0]] (N1 lower, in shared memory) into registers.
+template <typename R, int NX, int NY>
+SS_DEV void psi_rows(MC<R> c, const R* N1, R (&row)[(NX + NY + 31) / 32][Pad<R, NX + NY>::n]) {
+  typedef DS<R, NX, NY> S;
+  constexpr int W = S::W, CP = Pad<R, NX + NY>::n;
+  const int l = lane_id();
+  SS_UNROLL
+  for (int s = 0; s < (NX + NY + 31) / 32; ++s) {
+    const int r = l + 32 * s;
+    SS_UNROLL
+    for (int j = 0; j < CP; ++j) row[s][j] = R(0);
+    if (r < NY) {
+      R h[S::VN];
+      load_row<R, NX, S::LDN>(c.H, r, h);
+      SS_UNROLL
+      for (int k = 0; k < NX; ++k) {
+        SS_UNROLL
+        for (int j = 0; j <= k; j += W) {
+          const Vec<R> b = ld16(N1 + k * S::LDN + j);
+          SS_UNROLL
+          for (int u = 0; u < W; ++u) row[s][j + u] += h[k] * b.v[u];
+        }
+      }
+      SS_UNROLL
+      for (int j = 0; j < NY; j += W) {
+        const Vec<R> q = ld16(c.cR + r * S::LDY + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) row[s][NX + j + u] = q.v[u];
+      }
+    } else if (r < NY + NX) {
+      SS_UNROLL
+      for (int j = 0; j < NX; j += W) {
+        const Vec<R> q = ld16(N1 + (r - NY) * S::LDN + j);
+        SS_UNROLL
+        for (int u = 0; u < W; ++u) row[s][j + u] = q.v[u];
+      }
+    }
+  }
+}
+
 // Kalman steps of chunk c of every sequence: the factor recursion once, the
-// means as B rows.  Emits E, D (sequence 0's records) and g (every sequence's).
+// means as B rows.  Phi and Psi are built and triangularised in registers;
+// only Phi11 (= the predicted factor N1), E and Psi's blocks go through
+// shared memory.  Emits E, D (sequence 0's records) and g (every sequence's).
 template <typename R, int NX, int NY>
 __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
     walk_b_kernel(DenseArgs<R> a, int B, int64_t n_chunks, int64_t T) {
@@ -360,6 +443,9 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
   typedef DSS<R, NX, NY> SS;
   constexpr int WARPS = walk_b_warps<R, NX, NY>();
   constexpr int BR = SB_ROWS;
+  constexpr int W = S::W;
+  constexpr int NSF = (2 * NX + 31) / 32, CPF = Pad<R, 2 * NX>::n;
+  constexpr int NSP = (NX + NY + 31) / 32, CPP = Pad<R, NX + NY>::n;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   R* p = reinterpret_cast<R*>(smem_raw);
   const int warp = threadIdx.x >> 5, l = lane_id();
@@ -369,8 +455,9 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
   if (warp == 0) load_mc<R, NX, NY>(c, a);
   __syncthreads();
   R* L = p; p += S::MN;
-  R* Phi = p; p += S::MPHI;
-  R* Psi = Phi;
+  R* Eb = p; p += S::MN;
+  R* P11 = p; p += NY * S::LDY;
+  R* P21 = p; p += NX * S::LDY;
   R* Mv = p; p += SS::MB;
   R* MP = p; p += SS::MB;
   R* Gv = p; p += SS::MB;
@@ -386,13 +473,49 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
   load_rows<R, NX, NY>(Mv, st, n_chunks * S::ST, NX * NX, B);
   double ll = 0.0;
   for (int64_t t = t0; t < t1; ++t) {
-    // Phi = tria([[F L, cQ], [L, 0]]), E = Phi21 Phi11^{-1}, D = Phi22 (shared)
-    mm<R, NX, NX, NX, false, false, S::LDN, S::LDN, S::LD2, true>(Phi, c.F, L);
-    copy<R, NX, NX, false, S::LD2, S::LDN>(Phi + NX, c.cQ);
-    copy<R, NX, NX, false, S::LD2, S::LDN>(Phi + NX * S::LD2, L);
-    fill_diag<R, NX, NX, S::LD2>(Phi + NX * S::LD2 + NX, R(0));
-    tria<R, 2 * NX, 2 * NX, S::LD2>(Phi, vb);
-    trsm_rl<R, NX, NX, S::LD2, S::LD2>(Phi + NX * S::LD2, Phi);
+    R* rec = sa.selem + t * S::SE;
+    {
+      // Phi = tria([[F L, cQ], [L, 0]]): Phi11 -> L (= N1), E = Phi21 Phi11^{-1} -> Eb, D -> record
+      R row[NSF][CPF];
+      phi_rows<R, NX, NY>(c, L, row);
+      __syncwarp();
+      Tria<R, 2 * NX, 2 * NX, CPF>::run_regs(row, vb);
+      SS_UNROLL
+      for (int s = 0; s < NSF; ++s) {
+        const int r = l + 32 * s;
+        if (r < NX) store_part<R, NX, S::LDN, 0>(L, r, row[s]);
+      }
+      __syncwarp();
+      SS_UNROLL
+      for (int s = 0; s < NSF; ++s) {
+        const int r = l + 32 * s;
+        if (r >= NX && r < 2 * NX) {
+          SS_UNROLL
+          for (int k = NX - 1; k >= 0; --k) {
+            row[s][k] = row[s][k] / L[k * S::LDN + k];
+            SS_UNROLL
+            for (int jj = 0; jj < k; jj += W) {
+              const Vec<R> lv = ld16(L + k * S::LDN + jj);
+              SS_UNROLL
+              for (int u = 0; u < W; ++u)
+                if (jj + u < k) row[s][jj + u] -= row[s][k] * lv.v[u];
+            }
+          }
+          store_part<R, NX, S::LDN, 0>(Eb, r - NX, row[s]);
+          if (sa.emit_smoother) {
+            R* dst = rec + NX * NX + (r - NX) * NX;
+            SS_UNROLL
+            for (int jj = 0; jj < NX; jj += W) {
+              Vec<R> o;
+              SS_UNROLL
+              for (int u = 0; u < W; ++u) o.v[u] = row[s][NX + jj + u];
+              st16(dst + jj, o);
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
     // MP = Mv F^T + bq, G = Mv - MP E^T (rows = sequences)
     mm<R, BR, NX, NX, false, true, S::LDN, S::LDN, S::LDN>(MP, Mv, c.F);
     if (l < B) {
@@ -401,20 +524,29 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
     }
     __syncwarp();
     copy<R, BR, NX, false, S::LDN, S::LDN>(Gv, Mv);
-    mm<R, BR, NX, NX, false, true, S::LDN, S::LD2, S::LDN>(Gv, MP, Phi + NX * S::LD2, R(-1), true);
+    mm<R, BR, NX, NX, false, true, S::LDN, S::LDN, S::LDN>(Gv, MP, Eb, R(-1), true);
     if (sa.emit_smoother) {
-      R* rec = sa.selem + t * S::SE;
-      s2g<R, NX, NX, S::LD2>(rec, Phi + NX * S::LD2);
-      s2g<R, NX, NX, S::LD2>(rec + NX * NX, Phi + NX * S::LD2 + NX);
+      s2g<R, NX, NX, S::LDN>(rec, Eb);
       store_rows<R, NX, NY>(rec, T * S::SE, 2 * NX * NX, Gv, B);
     }
-    copy<R, NX, NX, false, S::LDN, S::LD2>(L, Phi);   // predicted factor
-    // Psi = tria([[H N1, cR], [N1, 0]]) (shared)
-    mm<R, NY, NX, NX, false, false, S::LDN, S::LDN, S::LDP, true>(Psi, c.H, L);
-    copy<R, NY, NY, false, S::LDP, S::LDY>(Psi + NX, c.cR);
-    copy<R, NX, NX, false, S::LDP, S::LDN>(Psi + NY * S::LDP, L);
-    fill_diag<R, NX, NY, S::LDP>(Psi + NY * S::LDP + NX, R(0));
-    tria<R, NX + NY, NX + NY, S::LDP>(Psi, vb);
+    {
+      // Psi = tria([[H N1, cR], [N1, 0]]): Psi11 -> P11, Psi21 -> P21, Psi22 -> L
+      R row[NSP][CPP];
+      psi_rows<R, NX, NY>(c, L, row);
+      __syncwarp();
+      Tria<R, NX + NY, NX + NY, CPP>::run_regs(row, vb);
+      SS_UNROLL
+      for (int s = 0; s < NSP; ++s) {
+        const int r = l + 32 * s;
+        if (r < NY) {
+          store_part<R, NY, S::LDY, 0>(P11, r, row[s]);
+        } else if (r < NY + NX) {
+          store_part<R, NY, S::LDY, 0>(P21, r - NY, row[s]);
+          store_part<R, NX, S::LDN, NY>(L, r - NY, row[s]);
+        }
+      }
+      __syncwarp();
+    }
     // residual rows r_i = y_i - c - H mp_i, z_i = Psi11^{-1} r_i
     mm<R, BR, NX, NY, false, true, S::LDN, S::LDN, S::LDY>(Rv, MP, c.H);
     if (l < B) {
@@ -424,21 +556,20 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
     }
     __syncwarp();
     copy<R, BR, NY, false, S::LDY, S::LDY>(Zv, Rv);
-    trsm_rlt<R, BR, NY, S::LDY, S::LDP>(Zv, Psi);
+    trsm_rlt<R, BR, NY, S::LDY, S::LDY>(Zv, P11);
     if (l < B) {
       R q = R(0), ld = R(0);
       SS_UNROLL
       for (int k = 0; k < NY; ++k) {
         const R z = Zv[l * S::LDY + k];
         q += z * z;
-        ld += ss_log(ss_abs(Psi[k * S::LDP + k]));
+        ld += ss_log(ss_abs(P11[k * S::LDY + k]));
       }
       ll += -0.5 * ((double)q + 2.0 * (double)ld);
     }
-    // Mv = MP + Z Psi21^T, L = Psi22
+    // Mv = MP + Z Psi21^T
     copy<R, BR, NX, false, S::LDN, S::LDN>(Mv, MP);
-    mm<R, BR, NY, NX, false, true, S::LDY, S::LDP, S::LDN>(Mv, Zv, Psi + NY * S::LDP, R(1), true);
-    copy<R, NX, NX, false, S::LDN, S::LDP>(L, Psi + NY * S::LDP + NY);
+    mm<R, BR, NY, NX, false, true, S::LDY, S::LDY, S::LDN>(Mv, Zv, P21, R(1), true);
     if (sa.filt_m != nullptr) {
       for (int i = 0; i < B; ++i) s2g<R, NX, NX, S::LDN>(sa.filt_L + ((int64_t)i * (T + 1) + t + 1) * NX * NX, L);
       store_rows<R, NX, NY>(sa.filt_m + (t + 1) * NX, (T + 1) * NX, 0, Mv, B);

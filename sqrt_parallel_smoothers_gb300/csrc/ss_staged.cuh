@@ -54,6 +54,19 @@ SS_DEV void unpack_se(const R (&r)[Rec<R, NX, 1>::SE_P], SElem<R, NX>& e) {
 }
 
 constexpr int STAGED_BLOCK = 128;
+// Minimum resident blocks per SM requested from the register allocator for the
+// per-step kernels.  The smoother walk fits three blocks without spilling and the
+// linearisation with a few words of spill; the filter leaf and walk hold a
+// 2nx x 2nx tria and would spill heavily below 255 registers.
+#ifndef SS_LIN_MINB
+#define SS_LIN_MINB 3
+#endif
+#ifndef SS_SWALK_MINB
+#define SS_SWALK_MINB 3
+#endif
+#ifndef SS_SCAN_MINB
+#define SS_SCAN_MINB 1
+#endif
 constexpr int STAGED_WARPS = STAGED_BLOCK / 32;
 
 // Dynamic shared memory (bytes) of each staged kernel.
@@ -74,7 +87,7 @@ SS_DEV R* warp_smem(unsigned char* raw, size_t warp_elems) {
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY, class TF, class OF, int METHOD>
-__global__ void __launch_bounds__(STAGED_BLOCK) lin_staged_kernel(LinArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(LinArgs<R> a) {
   typedef Rec<R, NX, NY> Q;
   extern __shared__ __align__(16) unsigned char ss_smem[];
   R* tile = warp_smem<R>(ss_smem, StageTile<R, Q::LIN>::WARP_ELEMS);
@@ -124,7 +137,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK) lin_staged_kernel(LinArgs<R> a) 
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY>
-__global__ void __launch_bounds__(STAGED_BLOCK) filter_leaf_staged_kernel(ScanArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_leaf_staged_kernel(ScanArgs<R> a) {
   typedef Rec<R, NX, NY> Q;
   typedef StageTile<R, Q::LIN> TL;
   extern __shared__ __align__(16) unsigned char ss_smem[];
@@ -172,7 +185,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK) filter_leaf_staged_kernel(ScanAr
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY>
-__global__ void __launch_bounds__(STAGED_BLOCK) filter_walk_staged_kernel(ScanArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged_kernel(ScanArgs<R> a) {
   typedef Rec<R, NX, NY> Q;
   typedef StageTile<R, Q::LIN> TL;
   typedef StageTile<R, Q::SE> TS;
@@ -237,7 +250,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK) filter_walk_staged_kernel(ScanAr
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX>
-__global__ void __launch_bounds__(STAGED_BLOCK) smoother_walk_staged_kernel(ScanArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, SS_SWALK_MINB) smoother_walk_staged_kernel(ScanArgs<R> a) {
   typedef Rec<R, NX, 1> Q;
   typedef StageTile<R, Q::SE> TS;
   constexpr int LW = (NX * NX) | 1;
