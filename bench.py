@@ -286,6 +286,28 @@ def adjoint_section(torch, S, flush):
             "max_rel_err": float(np.max(rel)), "method": "tangent-linear filter, one pass per parameter"}
 
 
+def rank_batch(S, batch_size, rank):
+    """Rank ``rank``'s share of a weak-scaling run: its own B sequences (the same length draw,
+    sequence i simulated from seed rank * B + i), independent of every other rank's."""
+    lengths = S.data.ragged_lengths(batch_size, seed=0)
+    batch = S.data.bearings_batch(lengths, qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=rank * batch_size)
+    return lengths, batch
+
+
+def max_over_ranks(torch, dist, ms, device):
+    """The slowest rank's step time: the job's step time."""
+    if dist is None:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, sum_T, ms):
+    """Whole-job timesteps/s: every rank processes its own sum_T steps per step time."""
+    return world * sum_T / (ms * 1e-3)
+
+
 def cv_section(torch, S, flush):
     """Constant-velocity linear model (nx = 4, ny = 2, dt = 0.1, q = 0.1, R = 0.5 I, m0 = 0,
     P0 = I), T = 1000 from seed 0, FP64: one parallel square-root filter + RTS smoother pass
@@ -433,8 +455,7 @@ def gpu_arm(args):
         if dist is not None:
             dist.barrier()
 
-    lengths = S.data.ragged_lengths(args.batch, seed=0)
-    batch = S.data.bearings_batch(lengths, qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=rank * args.batch)
+    lengths, batch = rank_batch(S, args.batch, rank)
     offsets = batch["offsets"]
     tuning = None
     if args.chunk == 0 and not args.no_autotune:
@@ -452,13 +473,9 @@ def gpu_arm(args):
     step_ms, clocks = time_plan(torch, plan, args.steps, args.warmup, flush, sampler)
     torch.cuda.synchronize()
     barrier()
-    ms = float(np.mean(step_ms))
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, dist, float(np.mean(step_ms)), "cuda")
     sum_T = int(lengths.sum())
-    value = world * sum_T / (ms * 1e-3)
+    value = job_value(world, sum_T, ms)
     launches = plan.launches_per_run * args.steps
 
     # e2e: host observations in (pinned), the smoothed trajectory out (pinned), every step
@@ -474,8 +491,8 @@ def gpu_arm(args):
         plan.run_host(ys_host, m_host, L_host)
     e1.record()
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e = {"value": world * sum_T / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": int(ys_host.nbytes),
+    e2e_ms = max_over_ranks(torch, dist, e0.elapsed_time(e1) / args.steps, "cuda")
+    e2e = {"value": job_value(world, sum_T, e2e_ms), "unit": UNIT, "h2d_bytes_per_step": int(ys_host.nbytes),
            "d2h_bytes_per_step": int(m_host.nbytes + L_host.nbytes), "ms_per_step": e2e_ms,
            "path": "IteratedSmootherPlan.run_host: pinned host copy-in, graph replay, copy-out"}
     mean32 = m_host.numpy().astype(np.float64)

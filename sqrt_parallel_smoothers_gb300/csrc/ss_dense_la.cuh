@@ -121,15 +121,16 @@ SS_DEV void store_part(R* M, int r, const R (&x)[CPX]) {
 // Algorithm 5.1.1, with Parlett's formula for the sign-free reflector, so the
 // diagonal comes out non-negative without a second pass).
 //
-// Per pivot p the pivot lane publishes its row (16-byte stores) and the
-// squared norm of its part right of p (four partial sums) in one of two
-// alternating buffers, so one warp barrier per pivot suffices; each lane then
-// applies the reflector to its one or two rows with split accumulators.  The
-// published row keeps x_p; the reflector's v_p differs from it only at p,
-// which is corrected with one select over the eight pivots of the block.
-// Pivots are processed in blocks of eight so that every register index is
-// compile-time.  vb holds two buffers of Pad<COLS>::n + W elements (16-byte
-// aligned): tria_scratch().
+// Per pivot p the pivot lane publishes its row x (16-byte stores, no masking)
+// and the squared norm of its part right of p (four partial sums) in one of
+// two alternating buffers, so one warp barrier per pivot suffices.  The
+// reflector v equals x right of p, v_p = x_p - ||x||-like (Parlett), zero left
+// of p; every lane forms row . v and row -= tau (row . v) v over the published
+// x and corrects the eight columns of the pivot block, the pivot row included
+// (it becomes (.., ||x||, ~0, ..) up to rounding).  The strict upper triangle
+// is cleared once at the end.  Pivots are processed in blocks of eight so that
+// every register index is compile-time.  vb holds two buffers of
+// Pad<COLS>::n + W elements (16-byte aligned): tria_scratch().
 template <typename R, int ROWS, int COLS, int LD>
 struct Tria {
   static constexpr int W = Vec<R>::n;
@@ -141,11 +142,12 @@ struct Tria {
 
   template <int J0>
   static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
+    constexpr int JB = (J0 + 8 < CP) ? J0 + 8 : CP;   // end of the pivot block's columns
     const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
     for (int p = J0; p < pend; ++p) {
       R* v = vb + (p & 1) * VS;
-      const int ps = p >> 5;
       if (lane == (p & 31)) {
+        const int ps = p >> 5;
         R sq[4] = {R(0), R(0), R(0), R(0)};
         SS_UNROLL
         for (int j = J0; j < CP; j += W) {
@@ -157,10 +159,9 @@ struct Tria {
             if constexpr (NS > 1) {
               if (ps == 1) xj = row[1][jj];
             }
-            const R m = (jj >= p && jj < COLS) ? xj : R(0);
-            o.v[u] = m;
-            const R q = (jj > p) ? m : R(0);
-            sq[jj & 3] += q * q;
+            o.v[u] = xj;
+            if (jj >= JB) sq[jj & 3] += xj * xj;
+            else if (jj > p) sq[jj & 3] += xj * xj;
           }
           st16(v + j, o);
         }
@@ -173,28 +174,22 @@ struct Tria {
       const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
       const R vv = v0 * v0 + sig;
       const R tau = (vv > R(0)) ? R(2) / vv : R(0);
-      const R dv = v0 - x0;   // v_p - x_p
-      if (lane == (p & 31)) {
+      // v - x on the pivot block: -x_j left of p, v_p - x_p at p, 0 right of p
+      R cb[JB - J0];
+      SS_UNROLL
+      for (int j = J0; j < JB; j += W) {
+        const Vec<R> x = ld16(v + j);
         SS_UNROLL
-        for (int s = 0; s < NS; ++s) {
-          if (s == ps) {
-            SS_UNROLL
-            for (int j = J0; j < CP; ++j) {
-              if (j == p) row[s][j] = nrm;
-              else if (j > p) row[s][j] = R(0);
-            }
-          }
+        for (int u = 0; u < W; ++u) {
+          const int jj = j + u;
+          cb[jj - J0] = (jj < p) ? -x.v[u] : ((jj == p) ? v0 - x0 : R(0));
         }
       }
-      R d[NS][4], rp[NS];
+      R d[NS][4];
       SS_UNROLL
       for (int s = 0; s < NS; ++s) {
         SS_UNROLL
         for (int k = 0; k < 4; ++k) d[s][k] = R(0);
-        rp[s] = R(0);
-        SS_UNROLL
-        for (int j = J0; j < J0 + 8 && j < CP; ++j)
-          if (j == p) rp[s] = row[s][j];
       }
       SS_UNROLL
       for (int j = J0; j < CP; j += W) {
@@ -202,30 +197,30 @@ struct Tria {
         SS_UNROLL
         for (int u = 0; u < W; ++u) {
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) d[s][(j + u) & 3] += row[s][j + u] * x.v[u];
+          for (int s = 0; s < NS; ++s) {
+            R vj = x.v[u];
+            if (j + u < JB) vj += cb[j + u - J0];
+            d[s][(j + u) & 3] += row[s][j + u] * vj;
+          }
         }
       }
       R f[NS];
       SS_UNROLL
       for (int s = 0; s < NS; ++s) {
         const int r = lane + 32 * s;
-        const R dd = (d[s][0] + d[s][1]) + (d[s][2] + d[s][3]) + rp[s] * dv;
-        f[s] = (r > p && r < ROWS) ? tau * dd : R(0);
+        const R dd = (d[s][0] + d[s][1]) + (d[s][2] + d[s][3]);
+        f[s] = (r >= p && r < ROWS) ? tau * dd : R(0);
       }
       SS_UNROLL
       for (int j = J0; j < CP; j += W) {
         const Vec<R> x = ld16(v + j);
         SS_UNROLL
         for (int u = 0; u < W; ++u) {
+          R vj = x.v[u];
+          if (j + u < JB) vj += cb[j + u - J0];
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) row[s][j + u] -= f[s] * x.v[u];
+          for (int s = 0; s < NS; ++s) row[s][j + u] -= f[s] * vj;
         }
-      }
-      SS_UNROLL
-      for (int s = 0; s < NS; ++s) {
-        SS_UNROLL
-        for (int j = J0; j < J0 + 8 && j < CP; ++j)
-          if (j == p) row[s][j] -= f[s] * dv;
       }
     }
   }
@@ -237,8 +232,20 @@ struct Tria {
 
   // The rows already in registers (row r = lane r % 32, slot r / 32; rows >= ROWS and
   // columns >= COLS zero).
+  static SS_DEV void clear_upper(R (&row)[NS][CP], int lane) {
+    SS_UNROLL
+    for (int s = 0; s < NS; ++s) {
+      const int r = lane + 32 * s;
+      SS_UNROLL
+      for (int j = 0; j < CP; ++j)
+        if (j > r) row[s][j] = R(0);
+    }
+  }
+
   static SS_DEV void run_regs(R (&row)[NS][CP], R* vb) {
-    blocks(row, vb, lane_id(), std::make_integer_sequence<int, (ROWS + 7) / 8>{});
+    const int lane = lane_id();
+    blocks(row, vb, lane, std::make_integer_sequence<int, (ROWS + 7) / 8>{});
+    clear_upper(row, lane);
     __syncwarp();
   }
 
@@ -256,6 +263,7 @@ struct Tria {
       }
     }
     blocks(row, vb, lane, std::make_integer_sequence<int, (ROWS + 7) / 8>{});
+    clear_upper(row, lane);
     SS_UNROLL
     for (int s = 0; s < NS; ++s) {
       const int r = lane + 32 * s;

@@ -31,9 +31,14 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
   static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
   SS_UNROLL
   for (int i = 0; i < ROWS; ++i) {
-    R sigma = R(0);
+    // two partial sums: halves the dependent chain of the norm
+    R sig0 = R(0), sig1 = R(0);
     SS_UNROLL
-    for (int j = i + 1; j < COLS; ++j) sigma += M[i][j] * M[i][j];
+    for (int j = i + 1; j < COLS; ++j) {
+      if ((j - i) & 1) sig0 += M[i][j] * M[i][j];
+      else sig1 += M[i][j] * M[i][j];
+    }
+    const R sigma = sig0 + sig1;
     const R x0 = M[i][i];
     R beta = x0;
     if (sigma != R(0)) {
@@ -47,10 +52,13 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
       for (int j = i + 1; j < COLS; ++j) v[j] = M[i][j] * inv;
       SS_UNROLL
       for (int r = i + 1; r < ROWS; ++r) {
-        R w = M[r][i];
+        R w0 = M[r][i], w1 = R(0);
         SS_UNROLL
-        for (int j = i + 1; j < COLS; ++j) w += M[r][j] * v[j];
-        w *= tau;
+        for (int j = i + 1; j < COLS; ++j) {
+          if ((j - i) & 1) w1 += M[r][j] * v[j];
+          else w0 += M[r][j] * v[j];
+        }
+        const R w = (w0 + w1) * tau;
         M[r][i] -= w;
         SS_UNROLL
         for (int j = i + 1; j < COLS; ++j) M[r][j] -= w * v[j];

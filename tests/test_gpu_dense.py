@@ -193,3 +193,23 @@ def test_dense_shared_equals_per_sequence(nx, ny, per_sequence_covariance):
     assert_rel(a.mean, b.mean, 1e-11, "means")
     assert_rel(cov(a.chol), cov(b.chol), 1e-11, "covariances")
     assert torch.equal(out[True][1]["iterations"], out[False][1]["iterations"])
+
+
+def test_dense_filter_prefix_at_full_size():
+    """The large-state workload's size (B = 16, T = 131 072, nx = 32, ny = 16, one prior), FP64:
+    filtering is causal, so each sequence's first 300 filtered states equal the oracle's
+    filter of its first 300 observations."""
+    sysm, (ot, oo), (gt, go) = _system(32, 16, seed=21)
+    F, Q, H, R, qm, rm = sysm
+    B, T, P = 16, 131_072, 300
+    rng = np.random.RandomState(5)
+    ys = rng.randn(B, T, 16)
+    ys[:, :P] = _observations(sysm, np.full(B, P), seed=5)
+    m0, L0 = _prior(32)
+    filt = S.filtering(torch.as_tensor(ys), S.MVNSqrt(torch.as_tensor(m0), torch.as_tensor(L0)), gt, go,
+                       S.linearization.extended, None, lengths=np.full(B, T), chunk=32)
+    for i in (0, B - 1):
+        ref = O.methods.filtering(ys[i, :P], O.MVNSqrt(m0, L0), ot, oo, O.linearization.extended, None, True)
+        assert_rel(filt.mean[i, :P + 1], ref.mean, 1e-9, f"seq {i} prefix mean")
+        assert_rel(cov(filt.chol[i, :P + 1]), cov(ref.chol), 1e-9, f"seq {i} prefix cov")
+    assert torch.isfinite(filt.mean).all()

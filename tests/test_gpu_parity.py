@@ -314,3 +314,23 @@ def test_robustness_loglikelihood_gpu(dtype):
         g = d["ell_extended"][ti]
         rel = np.abs(np_(ell) - g) / np.abs(g)
         assert np.mean(rel < 1e-4) >= 0.8, (T, rel)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-10), (torch.float32, 2e-3)])
+def test_filter_prefix_of_long_sequence(dtype, tol):
+    """Filtering is causal: the states of a T = 100 000 bearings filter (cubature at the prior
+    mean) up to step 1000 equal the oracle's filter of the first 1000 observations."""
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    T, P = 100_000, 1000
+    one = S.data.bearings_batch(np.array([T]), qc=0.1, qw=0.5, sigma=0.05, dt=0.01, seed0=77)
+    ys = one["ys"].astype(np.float64)
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    nom = S.MVNSqrt(torch.as_tensor(m0).expand(T + 1, 5).contiguous(),
+                    torch.eye(5, dtype=torch.float64).expand(T + 1, 5, 5).contiguous())
+    filt = S.filtering(torch.as_tensor(ys, dtype=dtype), S.MVNSqrt(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64)),
+                       gt, go, S.linearization.cubature, nom)
+    onom = O.MVNSqrt(np.repeat(m0[None], P + 1, 0), np.repeat(np.eye(5)[None], P + 1, 0))
+    ref = O.methods.filtering(ys[:P], O.MVNSqrt(m0, np.eye(5)), ot, oo, O.linearization.cubature, onom, True)
+    assert_rel(filt.mean[:P + 1], ref.mean, tol, "filtered mean prefix")
+    assert_rel(cov(filt.chol[:P + 1]), cov(ref.chol), tol, "filtered cov prefix")
+    assert torch.isfinite(filt.mean).all()
