@@ -200,6 +200,21 @@ int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void*
                    double* out_ell, double* out_grad, void* workspace, size_t workspace_bytes,
                    ss_stream_t stream);
 
+/* Log-likelihood of the iterated smoother and its derivatives along the same
+ * tangent directions: jax.grad of parsmooth.iterated_smoothing(...,
+ * return_loglikelihood=True) (parsmooth/methods.py:54-76 with the fixed-point
+ * VJP of parsmooth/_utils.py:113-133), as used for parameter estimation.  The
+ * n_iter-call loop (after the default-nominal pass when init_m is NULL) runs in
+ * tangent-linear arithmetic, so the tangent of each nominal trajectory enters
+ * the next linearisation; out_ell/out_grad are those of the filtering pass at
+ * the final nominal.  This is the exact derivative of the n_iter-call
+ * iteration, which tends to the implicit-function derivative as it converges. */
+int ss_iterated_grad_workspace_bytes(const ss_problem* p, size_t* bytes);
+int ss_iterated_grad(const ss_problem* p, const ss_tangents* tangents, const void* ys, const void* m0,
+                     const void* L0, int32_t prior_per_sequence, const void* init_m, const void* init_L,
+                     int32_t n_iter, double* out_ell, double* out_grad, void* workspace,
+                     size_t workspace_bytes, ss_stream_t stream);
+
 /* Instrumentation (no counterpart in the reference, which has no tracing):
  * a counter of kernels launched by this library, and per-kernel CUDA-event
  * timing.  While profiling is enabled every launch is bracketed by two events

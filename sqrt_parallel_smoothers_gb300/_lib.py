@@ -19,7 +19,7 @@ SS_OPT_PER_SEQUENCE_COVARIANCE = 1
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
             "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",
-            "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
+            "ss_iterated_grad", "ss_iterated_grad_workspace_bytes", "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
 
 
 class SSModel(ctypes.Structure):
@@ -79,6 +79,9 @@ def load():
         lib.ss_filter_grad_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
         lib.ss_filter_grad.argtypes = [PP, ctypes.POINTER(SSTangents), P, P, P, ctypes.c_int32, P, P, P, P, P,
                                        ctypes.c_size_t, P]
+        lib.ss_iterated_grad_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
+        lib.ss_iterated_grad.argtypes = [PP, ctypes.POINTER(SSTangents), P, P, P, ctypes.c_int32, P, P,
+                                         ctypes.c_int32, P, P, P, ctypes.c_size_t, P]
         lib.ss_profile_enable.argtypes = [ctypes.c_int]
         lib.ss_profile_read.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         for name in EXPORTED:

@@ -12,7 +12,8 @@ import os
 
 import torch
 
-DEFAULT_CANDIDATES = ((8, 8), (16, 8), (24, 8), (32, 8), (32, 4), (48, 8), (64, 8))
+DEFAULT_CANDIDATES = ((8, 8), (16, 8), (16, 4), (24, 4), (24, 8), (32, 2), (32, 4), (32, 8), (48, 4), (48, 8),
+                      (64, 4), (64, 8))
 
 
 def cache_path():

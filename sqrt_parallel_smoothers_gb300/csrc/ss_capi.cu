@@ -378,6 +378,55 @@ int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void*
   return f(c);
 }
 
+int ss_iterated_grad_workspace_bytes(const ss_problem* p, size_t* bytes) {
+  if (bytes == nullptr) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  RunFn f = find_grad(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_WORKSPACE;
+  c.p = p;
+  c.ws_bytes_out = bytes;
+  c.prior_per_sequence = 1;
+  c.n_iter = 1;  // the iterated layout
+  return f(c);
+}
+
+int ss_iterated_grad(const ss_problem* p, const ss_tangents* tangents, const void* ys, const void* m0,
+                     const void* L0, int32_t prior_per_sequence, const void* init_m, const void* init_L,
+                     int32_t n_iter, double* out_ell, double* out_grad, void* workspace,
+                     size_t workspace_bytes, ss_stream_t stream) {
+  if (p == nullptr || tangents == nullptr || m0 == nullptr || L0 == nullptr || out_ell == nullptr ||
+      out_grad == nullptr || n_iter < 1)
+    return SS_ERR_INVALID;
+  if (p->total_steps > 0 && ys == nullptr) return SS_ERR_INVALID;
+  if ((init_m == nullptr) != (init_L == nullptr)) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  RunFn f = find_grad(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_ITERATED;
+  c.p = p;
+  c.tangents = tangents;
+  c.ys = ys;
+  c.m0 = m0;
+  c.L0 = L0;
+  c.prior_per_sequence = prior_per_sequence;
+  c.nom_m = init_m;
+  c.nom_L = init_L;
+  c.n_iter = n_iter;
+  c.out_ell = out_ell;
+  c.out_grad = out_grad;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return f(c);
+}
+
 int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void* L0,
                 int32_t prior_per_sequence, const void* init_m, const void* init_L, int32_t n_iter,
                 double tol, void* out_m, void* out_L, double* out_ell, int32_t* out_iters,

@@ -21,6 +21,8 @@ struct Dual {
   }
   SS_DEV Dual(int x) : Dual(double(x)) {}
   SS_DEV Dual(float x) : Dual(double(x)) {}
+  // the value part (convergence tests and bookkeeping look at values only)
+  SS_DEV explicit operator double() const { return (double)v; }
   SS_DEV Dual& operator+=(const Dual& o) {
     v += o.v;
     SS_UNROLL

@@ -2,6 +2,14 @@
 // propagation: the whole filter pipeline instantiated on Dual<T, 1>, one
 // pass per parameter direction (a wider dual type multiplies the register
 // footprint of the square-root combines past what a thread can hold).
+//
+// The iterated form (OP_ITERATED) runs the whole fixed-point loop of
+// parsmooth/methods.py:54-76 in dual numbers, so the tangent of each nominal
+// trajectory is carried into the next call's linearisation, and returns the
+// derivative of the log-likelihood at the final nominal: the exact derivative
+// of the n_iter-call iteration, which tends to the implicit-function
+// derivative of the fixed point (parsmooth/_utils.py:113-133) as the
+// iteration converges.
 #pragma once
 #include "ss_run.cuh"
 
@@ -23,11 +31,11 @@ static __global__ void lift_kernel(const T* __restrict__ x, const T* __restrict_
 
 struct GradLayout {
   Layout inner;
-  size_t ys, m0, L0, nm, nL, tmat, omat, tqm, tqL, oqm, oqL, inner_base, bytes;
+  size_t ys, m0, L0, nm, nL, tmat, omat, tqm, tqL, oqm, oqL, om, oL, inner_base, bytes;
 };
 
 template <typename T, int NX, int NY>
-inline int make_grad_layout(const ss_problem& p, int64_t n_prior, GradLayout& g) {
+inline int make_grad_layout(const ss_problem& p, int64_t n_prior, bool iterated, GradLayout& g) {
   typedef Dual<T, GRAD_NT> D;
   int rc = make_layout<D, NX, NY>(p, g.inner);
   if (rc) return rc;
@@ -45,6 +53,8 @@ inline int make_grad_layout(const ss_problem& p, int64_t n_prior, GradLayout& g)
   g.tqL = take(NX * NX);
   g.oqm = take(NY);
   g.oqL = take(NY * NY);
+  g.om = take(iterated ? S * NX : 0);        // the iterated run's final trajectory (unused)
+  g.oL = take(iterated ? S * NX * NX : 0);
   g.inner_base = o;
   g.bytes = o + g.inner.bytes;
   return SS_OK;
@@ -66,8 +76,9 @@ int run_grad(const Call& c) {
   if (p.lin_method == SS_LIN_GAUSS_HERMITE) return SS_ERR_UNSUPPORTED;
   if (!models_supported<T, NX, NY>(p.transition.kind, p.observation.kind)) return SS_ERR_UNSUPPORTED;
   const int64_t n_prior = c.prior_per_sequence ? p.batch : 1;
+  const bool iterated = c.n_iter > 0;
   GradLayout g;
-  int rc = make_grad_layout<T, NX, NY>(p, n_prior, g);
+  int rc = make_grad_layout<T, NX, NY>(p, n_prior, iterated, g);
   if (rc) return rc;
   if (c.op == OP_WORKSPACE) {
     *c.ws_bytes_out = g.bytes;
@@ -125,7 +136,7 @@ int run_grad(const Call& c) {
       one.obs_params[0][k] = tg->obs_params[dir][k];
     }
     Call c2 = c;
-    c2.op = OP_FILTER;
+    c2.op = iterated ? OP_ITERATED : OP_FILTER;
     c2.p = &p2;
     c2.tangents = &one;
     c2.ys = w + g.ys;
@@ -133,14 +144,17 @@ int run_grad(const Call& c) {
     c2.L0 = w + g.L0;
     c2.nom_m = c.nom_m ? w + g.nm : nullptr;
     c2.nom_L = c.nom_m ? w + g.nL : nullptr;
-    c2.out_m = nullptr;
-    c2.out_L = nullptr;
+    c2.out_m = iterated ? w + g.om : nullptr;
+    c2.out_L = iterated ? w + g.oL : nullptr;
+    c2.tol = 0.0;
+    c2.out_iters = nullptr;
+    c2.out_flags = nullptr;
     c2.grad_ld = nd;
     c2.grad_col = dir;
     c2.ws = w + g.inner_base;
     c2.ws_bytes = g.inner.bytes;
     Runner<D, NX, NY> r(c2);
-    if ((rc = r.run_filter())) return rc;
+    if ((rc = iterated ? r.run_iterated() : r.run_filter())) return rc;
   }
   return SS_OK;
 }

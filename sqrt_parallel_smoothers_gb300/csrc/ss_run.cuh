@@ -155,6 +155,10 @@ inline void record_event(cudaEvent_t e, cudaStream_t st) {
     }                                                                      \
   } while (0)
 
+// The scan-level kernels (up, top, down) have few, long-running items; one warp
+// per block spreads them over every SM.
+constexpr int LEVEL_BLOCK = 32;
+
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block > 0 ? (n + block - 1) / block : 1); }
 
 // Lin-kernel dispatch over the model pair and method.
@@ -325,11 +329,11 @@ struct Runner {
   // Filter scan: level-1 summaries must already be in fsum[1] (filter_leaf).
   int filter_scan() {
     for (int l = 1; l < y.L; ++l) {
-      SS_LAUNCH("filter_up", st, filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
+      SS_LAUNCH("filter_up", st, filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
     }
-    SS_LAUNCH("filter_top", st, filter_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
+    SS_LAUNCH("filter_top", st, filter_top_kernel<R, NX><<<grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      SS_LAUNCH("filter_down", st, filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
+      SS_LAUNCH("filter_down", st, filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
     }
     return SS_OK;
   }
@@ -358,11 +362,11 @@ struct Runner {
 
   int smoother_scan_and_walk() {
     for (int l = 1; l < y.L; ++l) {
-      SS_LAUNCH("smoother_up", st, smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
+      SS_LAUNCH("smoother_up", st, smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
     }
-    SS_LAUNCH("smoother_top", st, smoother_top_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
+    SS_LAUNCH("smoother_top", st, smoother_top_kernel<R, NX><<<grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      SS_LAUNCH("smoother_down", st, smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], 128), 128, 0, st>>>(sa, l));
+      SS_LAUNCH("smoother_down", st, smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
     }
     if constexpr (Vec16<R>::vec) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::swalk;
@@ -459,7 +463,7 @@ struct Runner {
       sa.ll_chunk = at<double>(y.ll);
       rc = filter_pass(false);
       if (rc) return rc;
-      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, 1 + Tangents<R>::n, at<double>(y.ll), c.out_ell, nullptr, 0, 0, c.out_flags));
+      SS_LAUNCH("ll_reduce", st, ll_reduce_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NY, 1 + Tangents<R>::n, at<double>(y.ll), c.out_ell, c.out_grad, c.grad_ld, c.grad_col, c.out_flags));
     }
     if (c.out_iters || (c.out_flags && tol_mode)) {
       if (!tol_mode) {

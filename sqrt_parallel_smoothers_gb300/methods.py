@@ -394,11 +394,13 @@ def _filter_grad_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L
                     d_oqL: Optional[torch.Tensor], d_params: List[float], icfg: List[int], fcfg: List[float]
                     ) -> Tuple[torch.Tensor, torch.Tensor]:
     B, n_dir, per = icfg[10], icfg[14], icfg[13]
+    n_iter = icfg[15] if len(icfg) > 15 else 0
     dev = ys.device
     pr = _problem(icfg, fcfg, ys.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
     lib = _lib.load()
     nbytes = _lib.ctypes.c_size_t(0)
-    _lib.check(lib.ss_filter_grad_workspace_bytes(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
+    ws_query = lib.ss_iterated_grad_workspace_bytes if n_iter > 0 else lib.ss_filter_grad_workspace_bytes
+    _lib.check(ws_query(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
     ws = _workspace(nbytes.value, dev)
     tg = _lib.SSTangents()
     tg.n_dir = n_dir
@@ -411,9 +413,14 @@ def _filter_grad_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L
     tg.obs_noise_mean, tg.obs_noise_chol = _ptr(d_oqm), _ptr(d_oqL)
     ell = torch.empty((B,), dtype=torch.float64, device=dev)
     grad = torch.empty((B, n_dir), dtype=torch.float64, device=dev)
-    _lib.check(lib.ss_filter_grad(_lib.ctypes.byref(pr), _lib.ctypes.byref(tg), _ptr(ys), _ptr(m0), _ptr(L0), per,
-                                  _ptr(nom_m), _ptr(nom_L), _ptr(ell), _ptr(grad), _ptr(ws), nbytes.value,
-                                  _stream(dev)))
+    if n_iter > 0:
+        _lib.check(lib.ss_iterated_grad(_lib.ctypes.byref(pr), _lib.ctypes.byref(tg), _ptr(ys), _ptr(m0), _ptr(L0),
+                                        per, _ptr(nom_m), _ptr(nom_L), n_iter, _ptr(ell), _ptr(grad), _ptr(ws),
+                                        nbytes.value, _stream(dev)))
+    else:
+        _lib.check(lib.ss_filter_grad(_lib.ctypes.byref(pr), _lib.ctypes.byref(tg), _ptr(ys), _ptr(m0), _ptr(L0),
+                                      per, _ptr(nom_m), _ptr(nom_L), _ptr(ell), _ptr(grad), _ptr(ws), nbytes.value,
+                                      _stream(dev)))
     return ell, grad
 
 
@@ -736,13 +743,19 @@ class ModelTangent:
 
 def filter_loglikelihood_grad(observations, x0, transition_model, observation_model, linearization_method,
                               nominal_trajectory, directions, *, lengths=None, offsets=None, chunk=0, group=0,
-                              slr_form=0):
+                              slr_form=0, n_iter=0):
     """Log-likelihood of the parallel filter and its derivatives along parameter directions.
 
     ``directions``: list (at most 4) of ``(transition ModelTangent, observation ModelTangent)``.
     The filter (parsmooth/parallel/_filtering.py:13-61, return_loglikelihood) runs in
     tangent-linear arithmetic, one pass per direction, on the GPU.  Returns ``(ell, grad)``
-    (FP64), ``grad[..., k] = d ell / d theta_k``; per sequence for batches."""
+    (FP64), ``grad[..., k] = d ell / d theta_k``; per sequence for batches.
+
+    With ``n_iter > 0`` the function is instead the log-likelihood of the iterated smoother
+    (``iterated_smoothing(..., init_nominal_trajectory=nominal_trajectory, criterion=i < n_iter,
+    return_loglikelihood=True)``, parsmooth/methods.py:54-76): the whole loop runs in
+    tangent-linear arithmetic, so the nominal's dependence on the parameters is included (the
+    derivative parameter estimation takes through the fixed point, parsmooth/_utils.py:113-133)."""
     method = _check_common(x0, True, linearization_method)
     if nominal_trajectory is not None:
         are_inputs_compatible(x0, nominal_trajectory)
@@ -774,7 +787,7 @@ def filter_loglikelihood_grad(observations, x0, transition_model, observation_mo
     d_params = []
     for d in directions:
         d_params += [float(v) for v in d[0].params] + [float(v) for v in d[1].params]
-    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, [per, n_dir])
+    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, [per, n_dir, int(n_iter)])
     ell, grad = torch.ops.sqrtsmooth.filter_grad(lay.ys, lay.offsets, m0, L0, nm, nL, t_mat, t_qm, t_qL, o_mat,
                                                  o_qm, o_qL, d_tmat, d_omat, d_tqm, d_tqL, d_oqm, d_oqL, d_params,
                                                  icfg, _fcfg(method, fn_t, fn_o))
@@ -788,10 +801,13 @@ class BearingsLogLikelihood(torch.autograd.Function):
     ``Q(q) = q * Q1`` (``Q1`` the coordinated-turn noise at q = 1) and ``R = sigma^2 I``; the
     second sensor, the prior and the nominal trajectory are fixed.  The forward pass runs the
     GPU filter in tangent-linear arithmetic and keeps ``d ell / d theta``; backward is the
-    vector-Jacobian product.  ``ell`` is summed over the batch."""
+    vector-Jacobian product.  ``ell`` is summed over the batch.  With ``n_iter > 0`` the
+    log-likelihood is the iterated smoother's after ``n_iter`` calls from ``nominal`` (the
+    pseudo-log-likelihood of the reference's parameter estimation), differentiated through
+    the iterations."""
 
     @staticmethod
-    def forward(ctx, theta, observations, x0, nominal, Q1, dt, s2, method, lengths, offsets):
+    def forward(ctx, theta, observations, x0, nominal, Q1, dt, s2, method, lengths, offsets, n_iter=0):
         from .models import Bearings, CoordinatedTurn
         th = theta.detach().double().cpu()
         s1 = (float(th[0]), float(th[1]))
@@ -805,11 +821,11 @@ class BearingsLogLikelihood(torch.autograd.Function):
                 (ModelTangent(noise_chol=0.5 * cQ), ModelTangent()),
                 (ModelTangent(), ModelTangent(noise_chol=cR))]
         ell, grad = filter_loglikelihood_grad(observations, x0, tm, om, method, nominal, dirs, lengths=lengths,
-                                              offsets=offsets)
+                                              offsets=offsets, n_iter=n_iter)
         ctx.save_for_backward(grad.reshape(-1, 4).sum(0).to(device=theta.device, dtype=theta.dtype))
         return ell.sum().to(device=theta.device, dtype=theta.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):
         (g,) = ctx.saved_tensors
-        return (grad_out * g.to(grad_out.device),) + (None,) * 9
+        return (grad_out * g.to(grad_out.device),) + (None,) * 10

@@ -105,3 +105,54 @@ def test_bearings_theta_gradient_autograd(dtype, tol):
     g = theta.grad.numpy()
     rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1.0)
     assert np.all(rel <= tol), (g, fd, rel)
+
+
+def _bearings_iterated_ell_oracle(theta, ys, m0, nom, Q1, n_iter, dt=0.01, s2=(1.0, 1.0)):
+    s1 = (theta[0], theta[1])
+    q, sigma = np.exp(theta[2]), np.exp(theta[3])
+    tm = O.FunctionalModel(O.models.CoordinatedTurn(dt), O.MVNSqrt(np.zeros(5), np.linalg.cholesky(q * Q1)))
+    om = O.FunctionalModel(O.models.Bearings(s1, s2), O.MVNSqrt(np.zeros(2), sigma * np.eye(2)))
+    _, ell = O.methods.iterated_smoothing(ys, O.MVNSqrt(m0, np.eye(5)), tm, om, O.linearization.cubature, nom,
+                                          True, criterion=lambda i, *_: i < n_iter, return_loglikelihood=True)
+    return ell
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-5), (torch.float32, 2e-3)])
+def test_bearings_theta_gradient_through_iterations(dtype, tol):
+    """d/dtheta of the iterated smoother's log-likelihood (5 Gauss-Newton calls, the nominal's
+    dependence on theta included) against central differences of the oracle's iterated
+    log-likelihood."""
+    T, n_iter = 150, 5
+    w = S.data.bearings_workload(T, seed=3)
+    Q1, _ = S.data.bearings_noise(1.0, 5.0, 0.05, 0.01)
+    ys = w["ys"].astype(np.float64)
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    nom_m = np.repeat(m0[None], T + 1, 0)
+    nom_L = np.repeat(np.eye(5)[None], T + 1, 0)
+    theta0 = np.array([-1.5, 0.5, np.log(0.1), np.log(0.05)])
+    h = 1e-4
+    fd = []
+    for k in range(4):
+        e = np.zeros(4)
+        e[k] = h
+        fd.append((_bearings_iterated_ell_oracle(theta0 + e, ys, m0, O.MVNSqrt(nom_m, nom_L), Q1, n_iter) -
+                   _bearings_iterated_ell_oracle(theta0 - e, ys, m0, O.MVNSqrt(nom_m, nom_L), Q1, n_iter)) / (2 * h))
+    fd = np.array(fd)
+    theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    ell = S.BearingsLogLikelihood.apply(theta, torch.as_tensor(ys, dtype=dtype),
+                                        S.MVNSqrt(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64)),
+                                        S.MVNSqrt(torch.as_tensor(nom_m), torch.as_tensor(nom_L)), Q1, 0.01,
+                                        (1.0, 1.0), S.linearization.cubature, None, None, n_iter)
+    ell_ref = _bearings_iterated_ell_oracle(theta0, ys, m0, O.MVNSqrt(nom_m, nom_L), Q1, n_iter)
+    assert abs(float(ell.detach()) - ell_ref) <= tol * abs(ell_ref)
+    ell.backward()
+    g = theta.grad.numpy()
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1.0)
+    assert np.all(rel <= tol), (g, fd, rel)
+    # the nominal's dependence matters: the fixed-nominal filter gradient differs
+    dirs_only = S.BearingsLogLikelihood.apply(theta.detach().clone().requires_grad_(True),
+                                              torch.as_tensor(ys, dtype=dtype),
+                                              S.MVNSqrt(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64)),
+                                              S.MVNSqrt(torch.as_tensor(nom_m), torch.as_tensor(nom_L)), Q1, 0.01,
+                                              (1.0, 1.0), S.linearization.cubature, None, None)
+    assert abs(float(dirs_only.detach()) - float(ell.detach())) > 1e-6 * abs(float(ell.detach()))
