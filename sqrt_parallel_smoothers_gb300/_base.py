@@ -4,7 +4,8 @@ from typing import Any, Callable, NamedTuple
 
 
 class MVNStandard(NamedTuple):
-    """Gaussian in covariance form.  Accepted for type checks only: the GPU path is square-root."""
+    """Gaussian ``N(mean, cov)`` in covariance form.  The GPU path factors ``cov`` (``L L^T``)
+    and computes in square-root form; covariance-form inputs give covariance-form outputs."""
     mean: Any
     cov: Any
 

@@ -13,7 +13,7 @@ Extensions over the reference:
 * the dtype of ``observations`` (float32 or float64) selects the arithmetic;
   log-likelihoods are accumulated and returned in float64.
 
-``parallel=False``, ``MVNStandard`` inputs, ``ConditionalMomentsModel`` and
+``parallel=False``, ``ConditionalMomentsModel`` and
 Python callables that are not device models raise ``NotImplementedError``.
 """
 from typing import List, Optional, Tuple
@@ -433,6 +433,36 @@ def _(ys, offsets, m0, L0, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, d
 
 # ----------------------------------------------------------------------------- public API
 
+def _factor(P):
+    """Lower-triangular L with L L^T = P (batched), non-negative diagonal.  Cholesky where it
+    succeeds; a positive semi-definite P whose Cholesky fails is factored through its
+    eigendecomposition and a QR, i.e. tria(V sqrt(w))."""
+    P = P if isinstance(P, torch.Tensor) else torch.as_tensor(P)
+    L, info = torch.linalg.cholesky_ex(P)
+    if bool((info != 0).any()):
+        w, V = torch.linalg.eigh(0.5 * (P + P.transpose(-1, -2)))
+        Sq = V * w.clamp_min(0).sqrt().unsqueeze(-2)
+        L = torch.linalg.qr(Sq.transpose(-1, -2), mode="r").R.transpose(-1, -2)
+        sg = torch.sign(torch.diagonal(L, dim1=-2, dim2=-1))
+        L = L * torch.where(sg == 0, torch.ones_like(sg), sg).unsqueeze(-2)
+    return L
+
+
+def _std_to_sqrt(x):
+    return None if x is None else MVNSqrt(x.mean, _factor(x.cov))
+
+
+def _sqrt_to_std(x):
+    L = x.chol
+    return MVNStandard(x.mean, L @ L.transpose(-1, -2))
+
+
+def _model_to_sqrt(model):
+    if isinstance(model, FunctionalModel) and isinstance(model.mvn, MVNStandard):
+        return FunctionalModel(model.function, _std_to_sqrt(model.mvn))
+    return model
+
+
 def _check_common(x0, parallel, method):
     if not parallel:
         raise NotImplementedError("only parallel=True is implemented on the GPU")
@@ -475,7 +505,21 @@ def _dummy_ny(nx):
 def filtering(observations, x0, transition_model, observation_model, linearization_method,
               nominal_trajectory=None, parallel=True, return_loglikelihood=False, *, lengths=None,
               offsets=None, chunk=0, group=0, slr_form=0):
-    """Parallel square-root filter (parsmooth/methods.py:14-26 -> parsmooth/parallel/_filtering.py:13-61)."""
+    """Parallel square-root filter (parsmooth/methods.py:14-26 -> parsmooth/parallel/_filtering.py:13-61).
+
+    Covariance-form inputs (``MVNStandard`` prior, nominal and model noises, the reference's
+    standard filter) are factored on the device, filtered by the square-root kernels and
+    returned as covariances."""
+    if isinstance(x0, MVNStandard):
+        if nominal_trajectory is not None:
+            are_inputs_compatible(x0, nominal_trajectory)
+        out = filtering(observations, _std_to_sqrt(x0), _model_to_sqrt(transition_model),
+                        _model_to_sqrt(observation_model), linearization_method, _std_to_sqrt(nominal_trajectory),
+                        parallel, return_loglikelihood, lengths=lengths, offsets=offsets, chunk=chunk, group=group,
+                        slr_form=slr_form)
+        if return_loglikelihood:
+            return _sqrt_to_std(out[0]), out[1]
+        return _sqrt_to_std(out)
     method = _check_common(x0, parallel, linearization_method)
     if nominal_trajectory is not None:
         are_inputs_compatible(x0, nominal_trajectory)
@@ -502,6 +546,13 @@ def smoothing(transition_model, filter_trajectory, linearization_method, nominal
 
     For batches pass ``lengths`` (padded trajectories ``(B, T+1, ...)``) or
     ``offsets`` (packed trajectories, offsets of the steps)."""
+    if isinstance(filter_trajectory, MVNStandard):
+        if nominal_trajectory is not None:
+            are_inputs_compatible(filter_trajectory, nominal_trajectory)
+        return _sqrt_to_std(smoothing(_model_to_sqrt(transition_model), _std_to_sqrt(filter_trajectory),
+                                      linearization_method, _std_to_sqrt(nominal_trajectory), parallel,
+                                      lengths=lengths, offsets=offsets, chunk=chunk, group=group,
+                                      slr_form=slr_form))
     method = _check_common(filter_trajectory, parallel, linearization_method)
     if nominal_trajectory is not None:
         are_inputs_compatible(filter_trajectory, nominal_trajectory)
@@ -553,7 +604,19 @@ def iterated_smoothing(observations, x0, transition_model, observation_model, li
     :class:`MeanSquaredChange` / :class:`FixedIterations`.  With
     ``return_info=True`` a dict with per-sequence ``iterations`` and status
     ``flags`` (1 non-finite output, 2 non-finite log-likelihood, 4 not
-    converged) is returned last."""
+    converged) is returned last.  Covariance-form inputs are factored and the result returned
+    as covariances (see :func:`filtering`)."""
+    if isinstance(x0, MVNStandard):
+        if init_nominal_trajectory is not None:
+            are_inputs_compatible(x0, init_nominal_trajectory)
+        out = iterated_smoothing(observations, _std_to_sqrt(x0), _model_to_sqrt(transition_model),
+                                 _model_to_sqrt(observation_model), linearization_method,
+                                 _std_to_sqrt(init_nominal_trajectory), parallel, criterion, return_loglikelihood,
+                                 lengths=lengths, offsets=offsets, chunk=chunk, group=group, slr_form=slr_form,
+                                 return_info=return_info)
+        if isinstance(out, tuple):
+            return (_sqrt_to_std(out[0]),) + tuple(out[1:])
+        return _sqrt_to_std(out)
     method = _check_common(x0, parallel, linearization_method)
     if init_nominal_trajectory is not None:
         are_inputs_compatible(x0, init_nominal_trajectory)
@@ -583,9 +646,11 @@ def linearize(model, x, method):
     """Linearise ``model`` at ``x`` (one point or a batch) with ``method`` on the GPU.
 
     Equivalent of ``method(model, x)`` in parsmooth/linearization/*.py."""
-    method = resolve(method)
     if isinstance(x, MVNStandard):
-        raise NotImplementedError("covariance-form inputs are not supported: use MVNSqrt")
+        # the reference's covariance-form linearisation returns (F, Q, b) with Q a covariance
+        F, L, b = linearize(_model_to_sqrt(model), _std_to_sqrt(x), method)
+        return F, L @ L.transpose(-1, -2), b
+    method = resolve(method)
     dev = _device()
     m = torch.as_tensor(x.mean) if not isinstance(x.mean, torch.Tensor) else x.mean
     dtype = m.dtype if m.dtype in _DT else torch.float32
