@@ -328,6 +328,68 @@ def cv_section(torch, S, flush):
             "ms": float(np.median(ms)), "timesteps_per_s": 1000 / (float(np.median(ms)) * 1e-3)}
 
 
+def published_runtime_section(torch, S, flush):
+    """The reference's own GPU runtime experiment (notebooks/experiment_bearing_only_GPU_runtime.ipynb):
+    bearings-only CT with r = 0.5, qc = 0.01, qw = 0.1, dt = 0.01, prior m0 = (-4, -1, 2, 7, 3),
+    P0 = I, 10 iterated-smoother calls from the nominal (-1, -1, 6, 4, 2) broadcast, FP64,
+    one sequence of T = 4096, square-root parallel form; beside the reference's published times
+    for T = 4096 (notebooks/new_outputs/rtx-GPU-all-methods.csv:11, GeForce RTX 3080 Ti:
+    cubature 0.3751 s, extended 0.3012 s)."""
+    T = 4096
+    one = S.data.bearings_batch(np.array([T]), qc=0.01, qw=0.1, sigma=0.5, dt=0.01, seed0=50_000)
+    Q, R = S.data.bearings_noise(0.01, 0.1, 0.5, 0.01)
+    d = torch.float64
+    tm = S.FunctionalModel(S.models.CoordinatedTurn(0.01),
+                           S.MVNSqrt(torch.zeros(5, dtype=d), torch.as_tensor(np.linalg.cholesky(Q))))
+    om = S.FunctionalModel(S.models.Bearings((-1.5, 0.5), (1.0, 1.0)),
+                           S.MVNSqrt(torch.zeros(2, dtype=d), torch.as_tensor(np.linalg.cholesky(R))))
+    m0 = torch.tensor([-4.0, -1.0, 2.0, 7.0, 3.0], dtype=d)
+    x0 = S.MVNSqrt(m0, torch.eye(5, dtype=d))
+    n0 = torch.tensor([-1.0, -1.0, 6.0, 4.0, 2.0], dtype=d)
+    nom = S.MVNSqrt(n0.expand(T + 1, 5).contiguous(), torch.eye(5, dtype=d).expand(T + 1, 5, 5).contiguous())
+    out = {"workload": "bearings CT r=0.5 qc=0.01 qw=0.1, T=4096, 10 calls from (-1,-1,6,4,2) broadcast, FP64, "
+                       "sqrt parallel"}
+    for name, meth in (("cubature", S.linearization.cubature), ("extended", S.linearization.extended)):
+        plan = S.IteratedSmootherPlan(torch.as_tensor(one["ys"], dtype=d), x0, tm, om, meth, nom,
+                                      criterion=S.FixedIterations(10), graph=True)
+        ms, _ = time_plan(torch, plan, 10, 3, flush)
+        out[name + "_s"] = float(np.median(ms)) * 1e-3
+        del plan
+    out["reference_published_s"] = {"cubature": 0.3751, "extended": 0.3012, "hardware": "GeForce RTX 3080 Ti"}
+    out["speedup_vs_published"] = {k: out["reference_published_s"][k] / out[k + "_s"] for k in ("cubature", "extended")}
+    return out
+
+
+def population_section(torch, S, flush):
+    """The reference's population experiment (notebooks/experiment-poisson.ipynb): a Ricker-map
+    transition and Poisson counts as conditional-moments models, nx = ny = 1, T = 128, a random
+    prior and nominal, 100 iterated-smoother calls, FP64 (the notebook enables x64), one CUDA
+    graph.  Beside it, the reference's own published GPU times for the same setting
+    (notebooks/outputs/GPU-population-model.csv, T = 128: parallel IEKS 0.1676 s, IPLS 0.1666 s
+    per run, covariance form; this run uses the square-root form)."""
+    T, lam, Q = 128, 10.0, np.array([[0.3 ** 2]])
+    _, ys = S.data.population_data(T)
+    rng = np.random.RandomState(0)
+    m0, c0 = rng.randn(1), rng.randn(1, 1)
+    mean_f, _, mean_h, _, chol_f, chol_h = S.models.population_parameters(lam, Q)
+    f = S.ConditionalMomentsModel(mean_f, chol_f)
+    h = S.ConditionalMomentsModel(mean_h, chol_h)
+    d = torch.float64
+    x0 = S.MVNSqrt(torch.as_tensor(m0), torch.as_tensor(np.abs(c0)))
+    nom = S.MVNSqrt(torch.as_tensor(rng.randn(T + 1, 1)), torch.ones(T + 1, 1, 1, dtype=d))
+    out = {"workload": "population (Ricker + Poisson conditional moments), T=128, 100 calls, FP64, one CUDA graph"}
+    for name, meth in (("ieks", S.linearization.extended), ("ipls", S.linearization.cubature)):
+        plan = S.IteratedSmootherPlan(torch.as_tensor(ys, dtype=d), x0, f, h, meth, nom,
+                                      criterion=S.FixedIterations(100), graph=True)
+        ms, _ = time_plan(torch, plan, 5, 3, flush)
+        out[name + "_s"] = float(np.median(ms)) * 1e-3
+        del plan
+    out["reference_published_s"] = {"ieks_par": 0.16761423110961915, "ipls_par": 0.16656035900115967}
+    out["speedup_vs_published"] = {"ieks": out["reference_published_s"]["ieks_par"] / out["ieks_s"],
+                                   "ipls": out["reference_published_s"]["ipls_par"] / out["ipls_s"]}
+    return out
+
+
 def sweep_section(torch, S, flush):
     """Single-sequence bearings smoother (10 calls from the prior mean broadcast) for
     T = 1e2 .. 1e5, FP64 then FP32: timesteps/s and the FP32 position RMSE against FP64's."""
@@ -605,6 +667,8 @@ def gpu_arm(args):
     line["adjoint"] = adjoint_section(torch, S, flush)
     if not args.no_extra:
         line["cv_fp64"] = cv_section(torch, S, flush)
+        line["population"] = population_section(torch, S, flush)
+        line["published_runtime"] = published_runtime_section(torch, S, flush)
         line["sweep_T"] = sweep_section(torch, S, flush)
         line["large_state"] = large_state_section(torch, S, flush)
 

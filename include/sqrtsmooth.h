@@ -52,7 +52,12 @@ enum {
 enum {
   SS_MODEL_LINEAR = 0,           /* f(x) = A x                       (tests/_lgssm.py:5-35) */
   SS_MODEL_COORDINATED_TURN = 1, /* CT transition, nx = 5            (tests/bearings/bearings_utils.py:7-44) */
-  SS_MODEL_BEARINGS = 2          /* two bearings atan2, ny = 2       (tests/bearings/bearings_utils.py:47-69) */
+  SS_MODEL_BEARINGS = 2,         /* two bearings atan2, ny = 2       (tests/bearings/bearings_utils.py:47-69) */
+  SS_MODEL_RICKER = 3,           /* f(x)_i = a + x_i - exp(x_i), params[0] = a
+                                    (notebooks/population_model.py:9-21, a = log 44.7) */
+  SS_MODEL_POISSON_EXP = 4       /* conditional moments, ny <= nx: E[y_k|x] = Var[y_k|x] = lam exp(x_k),
+                                    params[0] = lam (notebooks/population_model.py:83-118); the
+                                    observation noise arguments are ignored */
 };
 
 /* Sigma-point regression form (see ss_lin.cuh): 0 = automatic (the
@@ -199,6 +204,20 @@ int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void*
                    const void* L0, int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
                    double* out_ell, double* out_grad, void* workspace, size_t workspace_bytes,
                    ss_stream_t stream);
+
+/* Pathwise posterior sampler: parsmooth.sampling (parsmooth/methods.py:79-91,
+ * parsmooth/_pathwise_sampler.py:13-127).  From the filtered trajectory
+ * (filt_m, filt_L) and the transition linearised at the nominal (NULL: zero
+ * means / identity factors; the reference's default is the smoothed trajectory,
+ * which the caller passes), draws n_samples trajectories per sequence:
+ * x_T = m_T + L_T e_T, x_t = E_t x_{t+1} + g_t + D_t e_t (t < T), with
+ * (g_t, E_t, D_t) the square-root smoothing elements.  eps and out share the
+ * trajectory layout of the states, (sum (T_i + 1), n_samples, nx); eps holds
+ * standard normals (the reference draws eps[0] for the last state and eps[1 + t]
+ * for step t; here eps[t] drives step t and eps[T] the last state). */
+int ss_sample(const ss_problem* p, const void* filt_m, const void* filt_L, const void* nominal_m,
+              const void* nominal_L, int32_t n_samples, const void* eps, void* out, void* workspace,
+              size_t workspace_bytes, ss_stream_t stream);
 
 /* Log-likelihood of the iterated smoother and its derivatives along the same
  * tangent directions: jax.grad of parsmooth.iterated_smoothing(...,

@@ -16,7 +16,7 @@ log-likelihoods in ``notebooks/robustness_data``), which are copied into
 
 from .core import (tria, canon, cholesky_update, cholesky_update_many, mvn_loglikelihood,
                    solve_lower, solve_upper)
-from .types import MVNSqrt, MVNStandard, FunctionalModel
+from .types import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsModel
 from . import models, linearization, parallel, sequential, methods
 
 __all__ = ["tria", "canon", "cholesky_update", "cholesky_update_many", "mvn_loglikelihood",

@@ -10,7 +10,7 @@ import math
 import numpy as np
 
 from .core import tria, cholesky_update_many, mT, mv
-from .types import MVNSqrt, MVNStandard, are_inputs_compatible
+from .types import MVNSqrt, MVNStandard, ConditionalMomentsModel, are_inputs_compatible
 
 
 # ----------------------------------------------------------------------------- sigma points
@@ -92,6 +92,11 @@ class _Method:
     name = ""
 
     def __call__(self, model, x):
+        if isinstance(model, ConditionalMomentsModel):
+            c_m, c_cov_or_chol = model
+            if isinstance(x, MVNSqrt):
+                return self.sqrt_conditional(c_m, c_cov_or_chol, x)
+            return self.standard_conditional(c_m, c_cov_or_chol, x)
         f, q = model
         are_inputs_compatible(x, q)
         if isinstance(x, MVNSqrt):
@@ -116,6 +121,17 @@ class Extended(_Method):
         b = f(m) - mv(F, m) + q.mean
         cov = np.broadcast_to(q.cov, F.shape[:-2] + np.shape(q.cov)).copy()
         return F, cov, b
+
+    # parsmooth/linearization/_extended.py:43-56
+    def sqrt_conditional(self, c_m, c_chol, x):
+        m = np.asarray(x.mean, dtype=float)
+        F = c_m.jacobian(m)
+        return F, c_chol(m), c_m(m) - mv(F, m)
+
+    def standard_conditional(self, c_m, c_cov, x):
+        m = np.asarray(x.mean, dtype=float)
+        F = c_m.jacobian(m)
+        return F, c_cov(m), c_m(m) - mv(F, m)
 
 
 class _SigmaPointMethod(_Method):
@@ -153,6 +169,31 @@ class _SigmaPointMethod(_Method):
         chol_L = tria(np.concatenate([sqrt_phi, chol_q], axis=-1))
         chol_L = cholesky_update_many(chol_L, mT(F @ chol), -1.0)
         return F, chol_L, m_f - mv(F, m) + q.mean
+
+    # parsmooth/linearization/_sigma_points.py:25-60
+    def sqrt_conditional(self, c_m, c_chol, x):
+        m = np.asarray(x.mean, dtype=float)
+        chol = np.asarray(x.chol, dtype=float)
+        F, pts, wc, f_pts, m_f = self._common(c_m, m, chol)
+        sqrt_phi = tria(mT(np.sqrt(wc)[:, None] * (f_pts - m_f[..., None, :])))
+        chol_pts = c_chol(pts)                                     # (..., N, d, d)
+        temp = np.sqrt(wc)[:, None, None] * chol_pts
+        temp = np.swapaxes(temp, -3, -2)                           # (..., d, N, d)
+        temp = temp.reshape(temp.shape[:-2] + (-1,))               # (..., d, N d)
+        chol_L = tria(np.concatenate([sqrt_phi, temp], axis=-1))
+        chol_L = cholesky_update_many(chol_L, mT(F @ chol), -1.0)
+        return F, chol_L, m_f - mv(F, m)
+
+    def standard_conditional(self, c_m, c_cov, x):
+        m = np.asarray(x.mean, dtype=float)
+        cov = np.asarray(x.cov, dtype=float)
+        chol = np.linalg.cholesky(cov)
+        F, pts, wc, f_pts, m_f = self._common(c_m, m, chol)
+        v_f = np.einsum("k,...kij->...ij", wc, c_cov(pts))
+        d = f_pts - m_f[..., None, :]
+        phi = np.einsum("k,...ki,...kj->...ij", wc, d, d)
+        temp = F @ chol
+        return F, phi - temp @ mT(temp) + v_f, m_f - mv(F, m)
 
     def standard(self, f, x, q):
         m = np.asarray(x.mean, dtype=float)

@@ -125,3 +125,67 @@ def bearings_noise(qc, qw, r, dt):
                   [0, 0, 0, 0, dt * qw]])
     R = r ** 2 * np.eye(2)
     return Q, R
+
+
+class Ricker:
+    """``a + x - exp(x)`` elementwise (notebooks/population_model.py:9-35, a = log 44.7)."""
+
+    def __init__(self, a=np.log(44.7)):
+        self.a = float(a)
+
+    def __call__(self, x):
+        x = np.asarray(x, dtype=float)
+        return self.a + x - np.exp(x)
+
+    def jacobian(self, x):
+        x = np.asarray(x, dtype=float)
+        return np.eye(x.shape[-1]) * (1.0 - np.exp(x))[..., None, :]
+
+
+class ConstantCovariance:
+    """``x -> Q`` (and its Cholesky factor with ``chol=True``), batched
+    (notebooks/population_model.py:38-65)."""
+
+    def __init__(self, Q, chol=False):
+        Q = np.atleast_2d(np.asarray(Q, dtype=float))
+        self.M = np.linalg.cholesky(Q) if chol else Q
+
+    def __call__(self, x):
+        x = np.asarray(x, dtype=float)
+        return np.broadcast_to(self.M, x.shape[:-1] + self.M.shape).copy()
+
+
+class PoissonExpMean:
+    """``E[y | x] = lam exp(x)`` (notebooks/population_model.py:83-98)."""
+
+    def __init__(self, lam, d_out=1):
+        self.lam, self.d_out = float(lam), int(d_out)
+
+    def __call__(self, x):
+        x = np.asarray(x, dtype=float)
+        return self.lam * np.exp(x[..., :self.d_out])
+
+    def jacobian(self, x):
+        x = np.asarray(x, dtype=float)
+        J = np.zeros(x.shape[:-1] + (self.d_out, x.shape[-1]))
+        for k in range(self.d_out):
+            J[..., k, k] = self.lam * np.exp(x[..., k])
+        return J
+
+
+class PoissonExpCovariance:
+    """``Cov[y | x] = diag(lam exp(x))`` or its square root with ``chol=True``
+    (notebooks/population_model.py:101-118)."""
+
+    def __init__(self, lam, d_out=1, chol=False):
+        self.lam, self.d_out, self.chol = float(lam), int(d_out), chol
+
+    def __call__(self, x):
+        x = np.asarray(x, dtype=float)
+        v = self.lam * np.exp(x[..., :self.d_out])
+        if self.chol:
+            v = np.sqrt(v)
+        out = np.zeros(x.shape[:-1] + (self.d_out, self.d_out))
+        for k in range(self.d_out):
+            out[..., k, k] = v[..., k]
+        return out

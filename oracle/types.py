@@ -24,6 +24,12 @@ class FunctionalModel(NamedTuple):
     mvn: Any
 
 
+class ConditionalMomentsModel(NamedTuple):
+    """``E[y | x]`` and ``Cov[y | x]`` (or its Cholesky factor) as callables (parsmooth/_base.py:20-22)."""
+    conditional_mean: Callable
+    conditional_covariance_or_cholesky: Callable
+
+
 def are_inputs_compatible(*ys):
     """Raise ``TypeError`` unless consecutive inputs share a type (parsmooth/_base.py:25-30)."""
     types = [type(y) for y in ys]

@@ -12,14 +12,14 @@ from ._build import LIB
 SS_OK, SS_ERR_INVALID, SS_ERR_UNSUPPORTED, SS_ERR_CUDA, SS_ERR_WORKSPACE = 0, 1, 2, 3, 4
 SS_F32, SS_F64 = 0, 1
 SS_LIN_EXTENDED, SS_LIN_CUBATURE, SS_LIN_UNSCENTED, SS_LIN_GAUSS_HERMITE = 0, 1, 2, 3
-SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS = 0, 1, 2
+SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS, SS_MODEL_RICKER, SS_MODEL_POISSON_EXP = 0, 1, 2, 3, 4
 SS_MAX_GH_ORDER = 8
 SS_MAX_TANGENTS = 4
 SS_OPT_PER_SEQUENCE_COVARIANCE = 1
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
             "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",
-            "ss_iterated_grad", "ss_iterated_grad_workspace_bytes", "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
+            "ss_iterated_grad", "ss_iterated_grad_workspace_bytes", "ss_sample", "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
 
 
 class SSModel(ctypes.Structure):
@@ -82,6 +82,7 @@ def load():
         lib.ss_iterated_grad_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
         lib.ss_iterated_grad.argtypes = [PP, ctypes.POINTER(SSTangents), P, P, P, ctypes.c_int32, P, P,
                                          ctypes.c_int32, P, P, P, ctypes.c_size_t, P]
+        lib.ss_sample.argtypes = [PP, P, P, P, P, ctypes.c_int32, P, P, P, ctypes.c_size_t, P]
         lib.ss_profile_enable.argtypes = [ctypes.c_int]
         lib.ss_profile_read.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         for name in EXPORTED:

@@ -168,7 +168,7 @@ static int validate(const ss_problem* p) {
   for (const ss_model* m : ms) {
     if (m->noise_mean == nullptr || m->noise_chol == nullptr) return SS_ERR_INVALID;
     if (m->kind == SS_MODEL_LINEAR && m->matrix == nullptr) return SS_ERR_INVALID;
-    if (m->kind < SS_MODEL_LINEAR || m->kind > SS_MODEL_BEARINGS) return SS_ERR_UNSUPPORTED;
+    if (m->kind < SS_MODEL_LINEAR || m->kind > SS_MODEL_POISSON_EXP) return SS_ERR_UNSUPPORTED;
   }
   if (find_run(p->dtype, p->nx, p->ny) == nullptr) return SS_ERR_UNSUPPORTED;
   return SS_OK;
@@ -376,6 +376,29 @@ int ss_filter_grad(const ss_problem* p, const ss_tangents* tangents, const void*
   c.ws_bytes = workspace_bytes;
   c.stream = reinterpret_cast<cudaStream_t>(stream);
   return f(c);
+}
+
+int ss_sample(const ss_problem* p, const void* filt_m, const void* filt_L, const void* nominal_m,
+              const void* nominal_L, int32_t n_samples, const void* eps, void* out, void* workspace,
+              size_t workspace_bytes, ss_stream_t stream) {
+  if (p == nullptr || filt_m == nullptr || filt_L == nullptr || n_samples < 1 || eps == nullptr || out == nullptr)
+    return SS_ERR_INVALID;
+  if ((nominal_m == nullptr) != (nominal_L == nullptr)) return SS_ERR_INVALID;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_SAMPLE;
+  c.p = p;
+  c.in_m = filt_m;
+  c.in_L = filt_L;
+  c.nom_m = nominal_m;
+  c.nom_L = nominal_L;
+  c.n_samples = n_samples;
+  c.eps = eps;
+  c.out_m = out;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return dispatch(c);
 }
 
 int ss_iterated_grad_workspace_bytes(const ss_problem* p, size_t* bytes) {

@@ -1053,6 +1053,19 @@ __global__ void __launch_bounds__(32 * SELEM_WARPS) selem_kernel(DenseArgs<R> a)
   }
 }
 
+// The last state of each sequence of a given trajectory into fT (standalone
+// smoothing; also for sequences without steps).  One warp per sequence.
+template <typename R, int NX, int NY>
+__global__ void __launch_bounds__(32) last_state_kernel(DenseArgs<R> a) {
+  typedef DS<R, NX, NY> S;
+  const ScanArgs<R>& sa = a.s;
+  const int64_t i = blockIdx.x;
+  if (i >= sa.g.B) return;
+  const int64_t s = sa.g.off[i + 1] + i;
+  g2g<R>(sa.fT + i * S::ST, sa.in_L + s * NX * NX, NX * NX);
+  g2g<R>(sa.fT + i * S::ST + NX * NX, sa.in_m + s * NX, NX);
+}
+
 // Exact linearisation of a linear model at n points (ss_linearize): F = A,
 // chol = qc (extended) or tria(qc) (the sigma-point rules' residual
 // covariance is zero), b = qm.  One warp per point.

@@ -269,6 +269,7 @@ struct DRunner {
     const size_t sm = sizeof(R) * (mc_elems<R, NX, NY>() + SELEM_WARPS * selem_warp_elems<R, NX, NY>());
     set_smem(selem_kernel<R, NX, NY>, sm);
     SS_LAUNCH("smoother_elements", st, selem_kernel<R, NX, NY><<<grid_for(y.items[1], SELEM_WARPS), 32 * SELEM_WARPS, sm, st>>>(a));
+    SS_LAUNCH("last_state", st, last_state_kernel<R, NX, NY><<<(unsigned)p.batch, 32, 0, st>>>(a));
     return smoother_pass();
   }
 
@@ -379,6 +380,7 @@ int run(const Call& c) {
     case OP_FILTER: return r.run_filter();
     case OP_SMOOTH: return r.run_smooth();
     case OP_ITERATED: return r.run_iterated();
+    case OP_SAMPLE: return SS_ERR_UNSUPPORTED;
     default: return SS_ERR_INVALID;
   }
 }

@@ -85,8 +85,17 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
     sc = ss_sqrt(R(DIN));
     w = R(1) / R(2 * DIN);
   }
+  // conditional-moments models (parsmooth/linearization/_sigma_points.py:25-60): the noise
+  // columns are the points' weighted conditional factors sqrt(wc_k) chol(Cov[y | x_k])
+  constexpr bool COND = IsConditional<Fn>::value;
+  constexpr int NQ = COND ? (NC + 2 * DIN) * DOUT : DOUT;   // noise columns
+  constexpr int NCP = COND ? DIN : 1;                       // stored conditional factors
   R fp[DIN][DOUT], fn[DIN][DOUT], f0[DOUT];
-  if constexpr (UT) f.eval(m, f0);
+  R cp[NCP][DOUT][DOUT], cn[NCP][DOUT][DOUT], c0[DOUT][DOUT];
+  if constexpr (UT) {
+    f.eval(m, f0);
+    if constexpr (COND) f.cond_chol(m, c0);
+  }
   SS_UNROLL
   for (int j = 0; j < DIN; ++j) {
     R xp[DIN], xn[DIN];
@@ -98,7 +107,26 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
     }
     f.eval(xp, fp[j]);
     f.eval(xn, fn[j]);
+    if constexpr (COND) {
+      f.cond_chol(xp, cp[j]);
+      f.cond_chol(xn, cn[j]);
+    }
   }
+  // noise column q of output row i
+  auto noise_col = [&](int i, int q) -> R {
+    if constexpr (COND) {
+      const int k = q / DOUT, jj = q - k * DOUT;   // point k: [centre], +0, -0, +1, -1, ...
+      if constexpr (UT) {
+        if (k == 0) return ss_sqrt(wc0) * c0[i][jj];
+      }
+      const int pk = k - NC;
+      const int j = pk >> 1;
+      const R sw = ss_sqrt(w);
+      return (pk & 1) ? sw * cn[j][i][jj] : sw * cp[j][i][jj];
+    } else {
+      return qc[i][q];
+    }
+  };
   R mf[DOUT];
   SS_UNROLL
   for (int i = 0; i < DOUT; ++i) {
@@ -130,7 +158,7 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
     }
   }
   if (slr_form == SS_SLR_RESIDUAL) {
-    constexpr int NCOL = NC + DIN + DOUT;
+    constexpr int NCOL = NC + DIN + NQ;
     R M[DOUT][NCOL];
     const R s2w = ss_sqrt(R(2) * w);
     SS_UNROLL
@@ -139,7 +167,7 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
       SS_UNROLL
       for (int j = 0; j < DIN; ++j) M[i][NC + j] = s2w * (R(0.5) * (fp[j][i] + fn[j][i]) - mf[i]);
       SS_UNROLL
-      for (int j = 0; j < DOUT; ++j) M[i][NC + DIN + j] = qc[i][j];
+      for (int q = 0; q < NQ; ++q) M[i][NC + DIN + q] = noise_col(i, q);
     }
     tria<R, DOUT, NCOL>(M);
     SS_UNROLL
@@ -148,7 +176,7 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
       for (int j = 0; j < DOUT; ++j) L[i][j] = (j <= i) ? M[i][j] : R(0);
     }
   } else {
-    constexpr int NCOL = NC + 2 * DIN + DOUT;
+    constexpr int NCOL = NC + 2 * DIN + NQ;
     R M[DOUT][NCOL];
     const R sw = ss_sqrt(w);
     SS_UNROLL
@@ -160,7 +188,7 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
         M[i][NC + DIN + j] = sw * (fn[j][i] - mf[i]);
       }
       SS_UNROLL
-      for (int j = 0; j < DOUT; ++j) M[i][NC + 2 * DIN + j] = qc[i][j];
+      for (int q = 0; q < NQ; ++q) M[i][NC + 2 * DIN + q] = noise_col(i, q);
     }
     tria<R, DOUT, NCOL>(M);
     SS_UNROLL
@@ -179,7 +207,7 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
   }
   SS_UNROLL
   for (int i = 0; i < DOUT; ++i) {
-    R s = mf[i] + qm[i];
+    R s = COND ? mf[i] : mf[i] + qm[i];
     SS_UNROLL
     for (int j = 0; j < DIN; ++j) s -= F[i][j] * m[j];
     b[i] = s;
@@ -192,17 +220,21 @@ SS_DEV void linearize(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], co
                       R (&F)[DOUT][DIN], R (&L)[DOUT][DOUT], R (&b)[DOUT]) {
   if constexpr (METHOD == SS_LIN_EXTENDED) {
     // parsmooth/linearization/_extended.py:59-70: F = df/dx(m), L = qc, b = f(m) - F m + qm
+    // (conditional models, _extended.py:43-56: chol = chol(Cov[y | m]), b = E[y | m] - F m)
+    constexpr bool COND = IsConditional<Fn>::value;
     f.jac(m, F);
     R fm[DOUT];
     f.eval(m, fm);
+    R cm[DOUT][DOUT];
+    if constexpr (COND) f.cond_chol(m, cm);
     SS_UNROLL
     for (int i = 0; i < DOUT; ++i) {
-      R s = fm[i] + qm[i];
+      R s = COND ? fm[i] : fm[i] + qm[i];
       SS_UNROLL
       for (int j = 0; j < DIN; ++j) s -= F[i][j] * m[j];
       b[i] = s;
       SS_UNROLL
-      for (int j = 0; j < DOUT; ++j) L[i][j] = qc[i][j];
+      for (int j = 0; j < DOUT; ++j) L[i][j] = COND ? cm[i][j] : qc[i][j];
     }
   } else if constexpr (METHOD == SS_LIN_CUBATURE || METHOD == SS_LIN_UNSCENTED) {
     linearize_symmetric<R, DIN, DOUT, Fn, METHOD>(f, m, C, qm, qc, ru, slr_form, F, L, b);
@@ -319,13 +351,39 @@ SS_DEV void linearize(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], co
         chol_add_column<R, DOUT>(L, fx);
       }
     }
-    // L <- tria([L, qc])
-    SS_UNROLL
-    for (int j = 0; j < DOUT; ++j) {
-      R col[DOUT];
+    constexpr bool COND = IsConditional<Fn>::value;
+    if constexpr (COND) {
+      // L <- tria([L, sqrt(wc_k) chol(Cov[y | x_k]) for every point])
+#pragma unroll 1
+      for (int k = 0; k < np; ++k) {
+        R xi[DIN], x[DIN], wm, wc, ck[DOUT][DOUT];
+        sigma_point<R, DIN, METHOD>(ru, k, xi, wm, wc);
+        SS_UNROLL
+        for (int i = 0; i < DIN; ++i) {
+          R s = m[i];
+          SS_UNROLL
+          for (int j = 0; j <= i; ++j) s += C[i][j] * xi[j];
+          x[i] = s;
+        }
+        f.cond_chol(x, ck);
+        const R sw = ss_sqrt(wc);
+        SS_UNROLL
+        for (int j = 0; j < DOUT; ++j) {
+          R col[DOUT];
+          SS_UNROLL
+          for (int i = 0; i < DOUT; ++i) col[i] = sw * ck[i][j];
+          chol_add_column<R, DOUT>(L, col);
+        }
+      }
+    } else {
+      // L <- tria([L, qc])
       SS_UNROLL
-      for (int i = 0; i < DOUT; ++i) col[i] = qc[i][j];
-      chol_add_column<R, DOUT>(L, col);
+      for (int j = 0; j < DOUT; ++j) {
+        R col[DOUT];
+        SS_UNROLL
+        for (int i = 0; i < DOUT; ++i) col[i] = qc[i][j];
+        chol_add_column<R, DOUT>(L, col);
+      }
     }
     if (!residual) {
       // downdate by the columns of F C (= S)
@@ -339,7 +397,7 @@ SS_DEV void linearize(const Fn& f, const R (&m)[DIN], const R (&C)[DIN][DIN], co
     }
     SS_UNROLL
     for (int i = 0; i < DOUT; ++i) {
-      R s = mf[i] + qm[i];
+      R s = COND ? mf[i] : mf[i] + qm[i];
       SS_UNROLL
       for (int j = 0; j < DIN; ++j) s -= F[i][j] * m[j];
       b[i] = s;

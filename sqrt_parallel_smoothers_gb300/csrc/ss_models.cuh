@@ -14,6 +14,8 @@ SS_DEV double ss_sin(double x) { return sin(x); }
 SS_DEV float ss_cos(float x) { return cosf(x); }
 SS_DEV double ss_cos(double x) { return cos(x); }
 SS_DEV float ss_atan2(float y, float x) { return atan2f(y, x); }
+SS_DEV float ss_exp(float x) { return expf(x); }
+SS_DEV double ss_exp(double x) { return exp(x); }
 SS_DEV double ss_atan2(double y, double x) { return atan2(y, x); }
 template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_sin(const Dual<T, NT>& a) { return chain(a, ss_sin(a.v), ss_cos(a.v)); }
@@ -33,7 +35,19 @@ SS_DEV Dual<T, NT> ss_atan2(const Dual<T, NT>& y, const Dual<T, NT>& x) {
 template <typename R>
 struct ModelArgs {
   const R* mat;   // LINEAR: d_out x d_in row-major matrix
-  R p[4];         // COORDINATED_TURN: p[0] = dt; BEARINGS: s1x, s1y, s2x, s2y
+  R p[4];         // COORDINATED_TURN: p[0] = dt; BEARINGS: s1x, s1y, s2x, s2y; RICKER: a; POISSON_EXP: lam
+};
+
+// A functor is a conditional-moments model (parsmooth/_base.py:20-22) when it
+// defines kConditional = true: eval gives E[y|x] and cond_chol a factor of
+// Cov[y|x]; its linearisation then ignores the model's additive noise.
+template <class Fn, class = void>
+struct IsConditional {
+  static constexpr bool value = false;
+};
+template <class Fn>
+struct IsConditional<Fn, decltype(void(Fn::kConditional))> {
+  static constexpr bool value = Fn::kConditional;
 };
 
 // f(x) = A x  (tests/_lgssm.py:5-35 in the reference)
@@ -128,6 +142,54 @@ struct BearingsFn {
       for (int j = 0; j < DIN; ++j) J[k][j] = R(0);
       J[k][0] = -dy / r2;
       J[k][1] = dx / r2;
+    }
+  }
+};
+
+// Ricker map on the log scale (notebooks/population_model.py:9-21), elementwise:
+// f(x)_i = a + x_i - exp(x_i).
+template <typename R, int DIN, int DOUT>
+struct RickerFn {
+  static_assert(DIN == DOUT, "the Ricker map is n -> n");
+  R a;
+  SS_DEV void init(const ModelArgs<R>& m) { a = m.p[0]; }
+  SS_DEV void eval(const R (&x)[DIN], R (&y)[DOUT]) const {
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) y[i] = a + x[i] - ss_exp(x[i]);
+  }
+  SS_DEV void jac(const R (&x)[DIN], R (&J)[DOUT][DIN]) const {
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DIN; ++j) J[i][j] = (i == j) ? R(1) - ss_exp(x[i]) : R(0);
+    }
+  }
+};
+
+// Poisson counts with log-intensity x (notebooks/population_model.py:83-118):
+// E[y_k | x] = Var[y_k | x] = lam exp(x_k), k < ny, as conditional moments.
+template <typename R, int DIN, int DOUT>
+struct PoissonExpFn {
+  static_assert(DOUT <= DIN, "one count per leading state component");
+  static constexpr bool kConditional = true;
+  R lam;
+  SS_DEV void init(const ModelArgs<R>& m) { lam = m.p[0]; }
+  SS_DEV void eval(const R (&x)[DIN], R (&y)[DOUT]) const {
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) y[i] = lam * ss_exp(x[i]);
+  }
+  SS_DEV void jac(const R (&x)[DIN], R (&J)[DOUT][DIN]) const {
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DIN; ++j) J[i][j] = (i == j) ? lam * ss_exp(x[i]) : R(0);
+    }
+  }
+  SS_DEV void cond_chol(const R (&x)[DIN], R (&C)[DOUT][DOUT]) const {
+    SS_UNROLL
+    for (int i = 0; i < DOUT; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < DOUT; ++j) C[i][j] = (i == j) ? ss_sqrt(lam * ss_exp(x[i])) : R(0);
     }
   }
 };

@@ -679,6 +679,74 @@ __global__ void __launch_bounds__(128) smoother_walk_kernel(ScanArgs<R> a) {
   }
 }
 
+// The last state of each sequence of a given (filtered) trajectory into fT: the
+// start of a standalone smoothing pass, also for sequences without steps.
+template <typename R, int NX>
+__global__ void __launch_bounds__(128) last_state_kernel(ScanArgs<R> a) {
+  typedef Rec<R, NX, 1> Q;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.g.B) return;
+  State<R, NX> s;
+  load_traj<R, NX>(a.in_m, a.in_L, a.g.off[i + 1] + i, s);
+  store_st<R, NX>(a.fT + i * Q::ST_P, s);
+}
+
+// ----------------------------------------------------------------------------- pathwise sampler
+
+// Posterior trajectories of parsmooth/_pathwise_sampler.py:13-127: from the
+// last filtered state x_T = m_T + L_T e_T, then x_t = E_t x_{t+1} + g_t + D_t e_t
+// with (g_t, E_t, D_t) the per-step smoothing elements (the sampler's gain,
+// increment mean and increment factor, :107-127).  One thread per (sequence,
+// sample); e and x in the trajectory layout (state, sample, nx).
+template <typename R, int NX>
+__global__ void __launch_bounds__(128) sample_kernel(ScanArgs<R> a, int S, const R* __restrict__ eps,
+                                                     R* __restrict__ out) {
+  typedef Rec<R, NX, 1> Q;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.g.B * (int64_t)S) return;
+  const int64_t i = k / S;
+  const int64_t smp = k - i * S;
+  const int64_t base = a.g.off[i];
+  const int64_t T = a.g.off[i + 1] - base;
+  const int64_t s0 = base + i;   // state index of t = 0
+  State<R, NX> f;
+  load_st<R, NX>(a.fT + i * Q::ST_P, f);
+  R x[NX];
+  {
+    const R* e = eps + ((s0 + T) * S + smp) * NX;
+    R* o = out + ((s0 + T) * S + smp) * NX;
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = f.m[r];
+      SS_UNROLL
+      for (int c = 0; c <= r; ++c) v += f.L[r][c] * e[c];
+      x[r] = v;
+      o[r] = v;
+    }
+  }
+  for (int64_t t = T - 1; t >= 0; --t) {
+    SElem<R, NX> se;
+    load_se<R, NX>(a.selem + (base + t) * Q::SE_P, se);
+    const R* e = eps + ((s0 + t) * S + smp) * NX;
+    R* o = out + ((s0 + t) * S + smp) * NX;
+    R xn[NX];
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = se.g[r];
+      SS_UNROLL
+      for (int c = 0; c < NX; ++c) v += se.E[r][c] * x[c];
+      SS_UNROLL
+      for (int c = 0; c <= r; ++c) v += se.D[r][c] * e[c];
+      xn[r] = v;
+    }
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      x[r] = xn[r];
+      o[r] = xn[r];
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- finishing kernels
 
 // Per-sequence log-likelihood: sum of chunk partials plus the constant

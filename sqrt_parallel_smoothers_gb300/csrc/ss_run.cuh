@@ -7,7 +7,8 @@
 
 namespace ss {
 
-enum { OP_WORKSPACE = 0, OP_LINEARIZE = 1, OP_FILTER = 2, OP_SMOOTH = 3, OP_ITERATED = 4, OP_SUPPORTED = 5 };
+enum { OP_WORKSPACE = 0, OP_LINEARIZE = 1, OP_FILTER = 2, OP_SMOOTH = 3, OP_ITERATED = 4, OP_SUPPORTED = 5,
+       OP_SAMPLE = 6 };
 
 // One entry-point call, dtype-erased.
 struct Call {
@@ -45,6 +46,8 @@ struct Call {
   size_t ws_bytes;
   cudaStream_t stream;
   const ss_tangents* tangents;  // forward-mode directions of the model scalars (gradient runs)
+  int32_t n_samples;            // sampler: draws per sequence
+  const void* eps;              // sampler: standard normals (states, n_samples, nx)
 };
 
 typedef int (*RunFn)(const Call&);
@@ -193,10 +196,15 @@ constexpr bool ct_ok() { return NX == 5; }
 template <int NX, int NY>
 constexpr bool bearings_ok() { return NY == 2 && NX >= 2; }
 
+template <int NX, int NY>
+constexpr bool poisson_ok() { return NY <= NX; }
+
 template <typename R, int NX, int NY>
 inline bool models_supported(int tk, int ok) {
-  const bool t = tk == SS_MODEL_LINEAR || (tk == SS_MODEL_COORDINATED_TURN && ct_ok<NX>());
-  const bool o = ok == SS_MODEL_LINEAR || (ok == SS_MODEL_BEARINGS && bearings_ok<NX, NY>());
+  const bool t = tk == SS_MODEL_LINEAR || (tk == SS_MODEL_COORDINATED_TURN && ct_ok<NX>()) ||
+                 tk == SS_MODEL_RICKER;
+  const bool o = ok == SS_MODEL_LINEAR || (ok == SS_MODEL_BEARINGS && bearings_ok<NX, NY>()) ||
+                 (ok == SS_MODEL_POISSON_EXP && poisson_ok<NX, NY>());
   return t && o;
 }
 
@@ -205,6 +213,9 @@ inline int launch_lin_obs(const LinArgs<R>& a, int ok, int method, cudaStream_t 
   if (ok == SS_MODEL_LINEAR) return launch_lin_method<R, NX, NY, TF, LinearFn<R, NX, NY>>(a, method, st);
   if constexpr (bearings_ok<NX, NY>()) {
     if (ok == SS_MODEL_BEARINGS) return launch_lin_method<R, NX, NY, TF, BearingsFn<R, NX, NY>>(a, method, st);
+  }
+  if constexpr (poisson_ok<NX, NY>()) {
+    if (ok == SS_MODEL_POISSON_EXP) return launch_lin_method<R, NX, NY, TF, PoissonExpFn<R, NX, NY>>(a, method, st);
   }
   return SS_ERR_UNSUPPORTED;
 }
@@ -227,6 +238,7 @@ inline int launch_lin(const LinArgs<R>& a, int tk, int ok, int method, cudaStrea
       if (tk == SS_MODEL_COORDINATED_TURN)
         return launch_lin_obs<R, NX, NY, CoordinatedTurnFn<R, NX, NX>>(a, ok, method, st);
     }
+    if (tk == SS_MODEL_RICKER) return launch_lin_obs<R, NX, NY, RickerFn<R, NX, NX>>(a, ok, method, st);
     return SS_ERR_UNSUPPORTED;
   }
 }
@@ -405,7 +417,26 @@ struct Runner {
     sa.out_m = static_cast<R*>(c.out_m);
     sa.out_L = static_cast<R*>(c.out_L);
     SS_LAUNCH("smoother_leaf", st, smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    SS_LAUNCH("last_state", st, last_state_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
     return smoother_scan_and_walk();
+  }
+
+  // Pathwise sampler: the smoothing elements of the given filtered trajectory
+  // (smoother_leaf_kernel), then one backward recursion per (sequence, sample).
+  int run_sample() {
+    int rc = prepare();
+    if (rc) return rc;
+    rc = lin(static_cast<const R*>(c.nom_m), static_cast<const R*>(c.nom_L), nullptr, true);
+    if (rc) return rc;
+    sa.in_m = static_cast<const R*>(c.in_m);
+    sa.in_L = static_cast<const R*>(c.in_L);
+    SS_LAUNCH("smoother_leaf", st, smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
+    SS_LAUNCH("last_state", st, last_state_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
+    const int64_t n = p.batch * (int64_t)c.n_samples;
+    SS_LAUNCH("sample", st, sample_kernel<R, NX><<<grid_for(n, 128), 128, 0, st>>>(sa, c.n_samples,
+                                                                                     static_cast<const R*>(c.eps),
+                                                                                     static_cast<R*>(c.out_m)));
+    return SS_OK;
   }
 
   int run_iterated() {
@@ -498,11 +529,16 @@ struct Runner {
         if (mdl.kind == SS_MODEL_COORDINATED_TURN)
           return launch_points_method<R, NX, NX, CoordinatedTurnFn<R, NX, NX>>(a, p.lin_method, st);
       }
+      if (mdl.kind == SS_MODEL_RICKER) return launch_points_method<R, NX, NX, RickerFn<R, NX, NX>>(a, p.lin_method, st);
     } else {
       if (mdl.kind == SS_MODEL_LINEAR) return launch_points_method<R, NX, NY, LinearFn<R, NX, NY>>(a, p.lin_method, st);
       if constexpr (bearings_ok<NX, NY>()) {
         if (mdl.kind == SS_MODEL_BEARINGS)
           return launch_points_method<R, NX, NY, BearingsFn<R, NX, NY>>(a, p.lin_method, st);
+      }
+      if constexpr (poisson_ok<NX, NY>()) {
+        if (mdl.kind == SS_MODEL_POISSON_EXP)
+          return launch_points_method<R, NX, NY, PoissonExpFn<R, NX, NY>>(a, p.lin_method, st);
       }
     }
     return SS_ERR_UNSUPPORTED;
@@ -527,6 +563,9 @@ int run(const Call& c) {
     case OP_FILTER: return r.run_filter();
     case OP_SMOOTH: return r.run_smooth();
     case OP_ITERATED: return r.run_iterated();
+    case OP_SAMPLE:
+      if constexpr (Tangents<R>::n == 0) return r.run_sample();
+      else return SS_ERR_UNSUPPORTED;
     default: return SS_ERR_INVALID;
   }
 }

@@ -167,3 +167,17 @@ def large_state_model(nx=32, ny=16, seed=0):
     H = rng.randn(ny, nx) / np.sqrt(nx)
     R = 0.1 * np.eye(ny)
     return F, Q, H, R
+
+
+def population_data(T, Q=0.3 ** 2, lam=10.0, x0=np.log(7.0), seed=40):
+    """Stochastic Ricker map with Poisson counts (notebooks/population_model.py:172-208):
+    x_{t+1} = log 44.7 + x_t - exp(x_t) + N(0, Q), y_t ~ Poisson(lam exp(x_t)) for t = 1..T,
+    seeded with NumPy.  Returns ``(xs (T+1, 1), ys (T, 1))``."""
+    rng = np.random.RandomState(seed)
+    xs = np.empty((T + 1, 1))
+    ys = np.empty((T, 1))
+    xs[0] = x0
+    for t in range(T):
+        xs[t + 1] = np.log(44.7) + xs[t] - np.exp(xs[t]) + np.sqrt(Q) * rng.randn(1)
+        ys[t] = rng.poisson(lam * np.exp(xs[t + 1]))
+    return xs, ys

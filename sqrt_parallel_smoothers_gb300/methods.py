@@ -13,8 +13,9 @@ Extensions over the reference:
 * the dtype of ``observations`` (float32 or float64) selects the arithmetic;
   log-likelihoods are accumulated and returned in float64.
 
-``parallel=False``, ``ConditionalMomentsModel`` and
-Python callables that are not device models raise ``NotImplementedError``.
+``parallel=False`` and Python callables that are not device models raise
+``NotImplementedError``; a ``ConditionalMomentsModel`` must be built from the conditional
+moments of a device model (``models.PoissonExp``, ``models.population_parameters``).
 """
 from typing import List, Optional, Tuple
 
@@ -184,7 +185,13 @@ def _prior(x0, lay, nx):
 
 def _model_tensors(model, d_in, d_out, dtype, device, sqrt=True):
     if isinstance(model, ConditionalMomentsModel):
-        raise NotImplementedError("ConditionalMomentsModel is not supported by the GPU smoother")
+        from .models import conditional_owner
+        fn = conditional_owner(model)
+        if fn.d_out != d_out or fn.d_in != d_in:
+            raise ValueError(f"{fn!r} maps R^{fn.d_in} -> R^{fn.d_out}, expected R^{d_in} -> R^{d_out}")
+        qm = torch.zeros(d_out, dtype=dtype, device=device)
+        qL = _as(fn.noise_chol(), dtype, device).reshape(d_out, d_out).contiguous()
+        return fn, None, qm, qL
     if not isinstance(model, FunctionalModel):
         raise TypeError(f"expected a FunctionalModel, got {type(model).__name__}")
     fn = as_device_model(model.function)
@@ -325,6 +332,25 @@ def _smooth_op(filt_m: torch.Tensor, filt_L: torch.Tensor, offsets: torch.Tensor
 @_smooth_op.register_fake
 def _(filt_m, filt_L, offsets, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg):
     return torch.empty_like(filt_m), torch.empty_like(filt_L)
+
+
+@torch.library.custom_op("sqrtsmooth::sample", mutates_args=())
+def _sample_op(filt_m: torch.Tensor, filt_L: torch.Tensor, offsets: torch.Tensor, nom_m: Optional[torch.Tensor],
+               nom_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor], t_qm: torch.Tensor,
+               t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor, o_qL: torch.Tensor,
+               eps: torch.Tensor, icfg: List[int], fcfg: List[float]) -> torch.Tensor:
+    dev = filt_m.device
+    pr = _problem(icfg, fcfg, filt_m.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    ws, nbytes = _ws_for(pr, dev)
+    out = torch.empty_like(eps)
+    _lib.check(_lib.load().ss_sample(_lib.ctypes.byref(pr), _ptr(filt_m), _ptr(filt_L), _ptr(nom_m), _ptr(nom_L),
+                                     int(eps.shape[1]), _ptr(eps), _ptr(out), _ptr(ws), nbytes, _stream(dev)))
+    return out
+
+
+@_sample_op.register_fake
+def _(filt_m, filt_L, offsets, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, eps, icfg, fcfg):
+    return torch.empty_like(eps)
 
 
 @torch.library.custom_op("sqrtsmooth::iterated", mutates_args=())
@@ -584,6 +610,70 @@ def smoothing(transition_model, filter_trajectory, linearization_method, nominal
     return MVNSqrt(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_L, (nx, nx)))
 
 
+def sampling(key, n_samples, transition_model, filter_trajectory, linearization_method, nominal_trajectory=None,
+             parallel=True, *, lengths=None, offsets=None, eps=None, chunk=0, group=0, slr_form=0):
+    """Pathwise posterior sampler (parsmooth/methods.py:79-91, parsmooth/_pathwise_sampler.py:13-127).
+
+    Returns ``n_samples`` trajectories drawn from the smoothing posterior given the filtered
+    trajectory: ``(T+1, n_samples, nx)`` (or ``(B, T+1, n_samples, nx)`` for padded batches,
+    packed ``(sum (T_i+1), n_samples, nx)`` with ``offsets``).  ``key`` seeds the draws (an int
+    or a ``torch.Generator``); ``eps`` may instead give the standard normals in the
+    reference's order, shape ``(T+1, n_samples, nx)`` with ``eps[0]`` driving the last state
+    and ``eps[1 + t]`` step t (per sequence for batches).  The default nominal is the smoothed
+    trajectory, as in the reference.  The draws run on the GPU, one thread per (sequence,
+    sample) walking its trajectory backwards; ``parallel`` selects nothing (both of the
+    reference's forms give the same draws)."""
+    if isinstance(filter_trajectory, MVNStandard):
+        if nominal_trajectory is not None:
+            are_inputs_compatible(filter_trajectory, nominal_trajectory)
+        return sampling(key, n_samples, _model_to_sqrt(transition_model), _std_to_sqrt(filter_trajectory),
+                        linearization_method, _std_to_sqrt(nominal_trajectory), parallel, lengths=lengths,
+                        offsets=offsets, eps=eps, chunk=chunk, group=group, slr_form=slr_form)
+    if nominal_trajectory is None:
+        nominal_trajectory = smoothing(transition_model, filter_trajectory, linearization_method, None, parallel,
+                                       lengths=lengths, offsets=offsets, chunk=chunk, group=group,
+                                       slr_form=slr_form)
+    method = _check_common(filter_trajectory, True, linearization_method)
+    are_inputs_compatible(filter_trajectory, nominal_trajectory)
+    fm = filter_trajectory.mean if isinstance(filter_trajectory.mean, torch.Tensor) else \
+        torch.as_tensor(filter_trajectory.mean)
+    dtype = fm.dtype if fm.dtype in _DT else torch.float32
+    dev = _device()
+    nx = int(fm.shape[-1])
+    if offsets is not None:
+        off = torch.as_tensor(offsets, dtype=torch.int64)
+        lay = _Layout(torch.zeros((int(off[-1]), 1), dtype=dtype), None, off, dtype, dev)
+    elif fm.ndim == 2:
+        lay = _Layout(torch.zeros((fm.shape[0] - 1, 1), dtype=dtype), None, None, dtype, dev)
+    else:
+        B, Tp1 = fm.shape[:2]
+        lay = _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    ny = _dummy_ny(nx)
+    fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev, ny)
+    fmp = lay.pack_states(filter_trajectory.mean, (nx,))
+    fLp = _lower_batched(lay.pack_states(filter_trajectory.chol, (nx, nx)))
+    nm, nL = _nominal(nominal_trajectory, lay, nx)
+    n_samples = int(n_samples)
+    if eps is None:
+        gen = key if isinstance(key, torch.Generator) else torch.Generator(device=dev).manual_seed(int(key))
+        e = torch.randn((fmp.shape[0], n_samples, nx), generator=gen, dtype=lay.dtype, device=dev)
+    else:
+        # reference order per sequence (eps[0] last state, eps[1 + t] step t) -> state order
+        # (eps[t] step t, eps[T] last): state t of sequence i takes entry (t + 1) mod (T_i + 1)
+        e = lay.pack_states(torch.as_tensor(eps), (n_samples, nx))
+        off = lay.offsets.to(dev)
+        n_st = off[1:] - off[:-1] + 1
+        s0 = off[:-1] + torch.arange(off.shape[0] - 1, device=dev)
+        seq = torch.repeat_interleave(torch.arange(n_st.shape[0], device=dev), n_st)
+        t_in = torch.arange(e.shape[0], device=dev) - s0[seq]
+        e = e.index_select(0, s0[seq] + (t_in + 1) % n_st[seq]).contiguous()
+    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, [0, 0])
+    out = torch.ops.sqrtsmooth.sample(fmp, fLp, lay.offsets, nm, nL, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, e,
+                                      icfg, _fcfg(method, fn_t, fn_o))
+    return lay.unpack_states(out, (n_samples, nx))
+
+
 def filter_smoother(observations, x0, transition_model, observation_model, linearization_method,
                     nominal_trajectory=None, parallel=True, **kw):
     """parsmooth/methods.py:38-47."""
@@ -658,9 +748,13 @@ def linearize(model, x, method):
     nx = int(m.shape[-1])
     mm = _as(m, dtype, dev).reshape(-1, nx)
     LL = _lower_batched(_as(x.chol, dtype, dev).reshape(-1, nx, nx))
-    fn = as_device_model(model.function)
+    if isinstance(model, ConditionalMomentsModel):
+        from .models import conditional_owner
+        fn = conditional_owner(model)
+    else:
+        fn = as_device_model(model.function)
     d_out = fn.d_out
-    is_obs = not (d_out == nx and fn.kind != _lib.SS_MODEL_BEARINGS)
+    is_obs = not (d_out == nx and fn.kind not in (_lib.SS_MODEL_BEARINGS, _lib.SS_MODEL_POISSON_EXP))
     fnm, mat, qm, qL = _model_tensors(model, nx, d_out, dtype, dev)
     if is_obs:
         fn_t, t_mat, t_qm, t_qL = _dummy_transition(nx, dtype, dev)
