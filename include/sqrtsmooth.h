@@ -194,9 +194,9 @@ typedef struct ss_tangents {
   const void* trans_matrix;           /* (n_dir, nx, nx) or NULL for zero, device */
   const void* obs_matrix;             /* (n_dir, ny, nx) or NULL */
   const void* trans_noise_mean;       /* (n_dir, nx) or NULL */
-  const void* trans_noise_chol;       /* (n_dir, nx, nx) or NULL */
+  const void* trans_noise_chol;       /* (n_dir, nx, nx) lower triangular, or NULL */
   const void* obs_noise_mean;         /* (n_dir, ny) or NULL */
-  const void* obs_noise_chol;         /* (n_dir, ny, ny) or NULL */
+  const void* obs_noise_chol;         /* (n_dir, ny, ny) lower triangular, or NULL */
 } ss_tangents;
 
 int ss_filter_grad_workspace_bytes(const ss_problem* p, size_t* bytes);

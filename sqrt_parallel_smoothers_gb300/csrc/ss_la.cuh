@@ -5,6 +5,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <type_traits>
 
 #define SS_DEV __device__ __forceinline__
 #define SS_UNROLL _Pragma("unroll")
@@ -75,6 +76,146 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
       M[i][i] = beta;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// tria_sp: the same factor as tria, for inputs with a known zero pattern.
+//
+// Every square-root step factors a block matrix whose blocks are full,
+// lower-triangular or zero ([[F L, cQ], [L, 0]] and the like).  A Householder
+// reflection from the right only spreads non-zeros within the columns it
+// touches, so the pattern of every intermediate matrix follows from the input
+// pattern alone.  TriaPlan runs that propagation at compile time: for each
+// reflector i, the columns > i it carries (sup) and the rows > i it changes
+// (touch).  The device loop then skips products with structural zeros.  The
+// skipped terms are exact zeros in tria's arithmetic (0 * v added to a partial
+// sum, a row updated by w = 0), and the partial sums alternate on the same
+// column parity, so the result equals tria's on finite inputs.
+//
+// PAT::nz(r, c) is true where the input may be non-zero; entries it calls zero
+// are taken as zero.
+template <int ROWS, int COLS>
+struct TriaPlan {
+  unsigned long long sup[ROWS];
+  unsigned long long touch[ROWS];
+};
+
+template <int ROWS, int COLS, class PAT>
+__host__ __device__ constexpr TriaPlan<ROWS, COLS> make_tria_plan() {
+  static_assert(COLS <= 64 && ROWS <= 64, "patterns are 64-bit masks");
+  TriaPlan<ROWS, COLS> p{};
+  unsigned long long nz[ROWS] = {};
+  for (int r = 0; r < ROWS; ++r)
+    for (int c = 0; c < COLS; ++c)
+      if (PAT::nz(r, c)) nz[r] |= 1ull << c;
+  for (int i = 0; i < ROWS; ++i) {
+    const unsigned long long below = (i + 1 < 64) ? ~((2ull << i) - 1) : 0ull;
+    const unsigned long long s = nz[i] & below;
+    const unsigned long long cols = s | (1ull << i);
+    p.sup[i] = s;
+    p.touch[i] = 0;
+    if (s != 0) {
+      for (int r = i + 1; r < ROWS; ++r) {
+        if (nz[r] & cols) {
+          p.touch[i] |= 1ull << r;
+          nz[r] |= cols;
+        }
+      }
+    }
+    nz[i] = 1ull << i;
+  }
+  return p;
+}
+
+// Block patterns.  Rows [0, RT) over columns [0, CL) are full; rows [0, RT)
+// over columns [CL, COLS) are lower triangular with KB leading full columns
+// (entry (r, CL + c) non-zero iff c <= r or c < KB); rows [RT, ROWS) are lower
+// triangular (full when BL_FULL) over columns [0, CL) and zero beyond.
+template <int RT, int CL, int KB = 0, bool BL_FULL = false>
+struct PatBlocks {
+  __host__ __device__ static constexpr bool nz(int r, int c) {
+    if (r < RT) return c < CL || (c - CL) <= r || (c - CL) < KB;
+    return c < CL && (BL_FULL || c <= r - RT);
+  }
+};
+
+struct PatFull {
+  __host__ __device__ static constexpr bool nz(int, int) { return true; }
+};
+
+template <typename R, int ROWS, int COLS, class PAT, int I>
+SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
+  if constexpr (I < ROWS) {
+    constexpr TriaPlan<ROWS, COLS> P = make_tria_plan<ROWS, COLS, PAT>();
+    constexpr unsigned long long SUP = P.sup[I];
+    constexpr unsigned long long TOUCH = P.touch[I];
+    constexpr int i = I;
+    R beta = M[i][i];
+    if constexpr (SUP != 0) {
+      R sig0 = R(0), sig1 = R(0);
+      SS_UNROLL
+      for (int j = i + 1; j < COLS; ++j) {
+        if ((SUP >> j) & 1) {
+          if ((j - i) & 1) sig0 += M[i][j] * M[i][j];
+          else sig1 += M[i][j] * M[i][j];
+        }
+      }
+      const R sigma = sig0 + sig1;
+      const R x0 = M[i][i];
+      if (sigma != R(0)) {
+        const R nrm = ss_sqrt(x0 * x0 + sigma);
+        beta = (x0 <= R(0)) ? nrm : -nrm;
+        const R v0 = x0 - beta;
+        const R tau = -v0 / beta;
+        const R inv = R(1) / v0;
+        R v[COLS];
+        SS_UNROLL
+        for (int j = i + 1; j < COLS; ++j)
+          if ((SUP >> j) & 1) v[j] = M[i][j] * inv;
+        SS_UNROLL
+        for (int r = i + 1; r < ROWS; ++r) {
+          if ((TOUCH >> r) & 1) {
+            R w0 = M[r][i], w1 = R(0);
+            SS_UNROLL
+            for (int j = i + 1; j < COLS; ++j) {
+              if ((SUP >> j) & 1) {
+                if ((j - i) & 1) w1 += M[r][j] * v[j];
+                else w0 += M[r][j] * v[j];
+              }
+            }
+            const R w = (w0 + w1) * tau;
+            M[r][i] -= w;
+            SS_UNROLL
+            for (int j = i + 1; j < COLS; ++j)
+              if ((SUP >> j) & 1) M[r][j] -= w * v[j];
+          }
+        }
+      }
+    }
+    SS_UNROLL
+    for (int j = i + 1; j < COLS; ++j) M[i][j] = R(0);
+    if (beta < R(0)) {
+      M[i][i] = -beta;
+      SS_UNROLL
+      for (int r = i + 1; r < ROWS; ++r) M[r][i] = -M[r][i];
+    } else {
+      M[i][i] = beta;
+    }
+    tria_sp_step<R, ROWS, COLS, PAT, I + 1>(M);
+  }
+}
+
+template <typename R, int ROWS, int COLS, class PAT>
+SS_DEV void tria_sp(R (&M)[ROWS][COLS]) {
+  static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
+  // entries outside the pattern are zero: say so, so that they cost no registers
+  SS_UNROLL
+  for (int r = 0; r < ROWS; ++r) {
+    SS_UNROLL
+    for (int c = 0; c < COLS; ++c)
+      if (!PAT::nz(r, c)) M[r][c] = R(0);
+  }
+  tria_sp_step<R, ROWS, COLS, PAT, 0>(M);
 }
 
 // ---------------------------------------------------------------------------
@@ -314,6 +455,17 @@ SS_DEV void unpack(const R (&rec)[P], int off, R (&A)[M][N]) {
   for (int i = 0; i < M; ++i) {
     SS_UNROLL
     for (int j = 0; j < N; ++j) A[i][j] = rec[off + i * N + j];
+  }
+}
+// Lower-triangular factor stored as a full square: the upper entries are
+// zero by construction, and setting them here lets the compiler treat them as
+// constants.
+template <typename R, int N, int P>
+SS_DEV void unpack_lower(const R (&rec)[P], int off, R (&A)[N][N]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) A[i][j] = (j <= i) ? rec[off + i * N + j] : R(0);
   }
 }
 template <typename R, int N, int P>

@@ -169,7 +169,9 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
       SS_UNROLL
       for (int q = 0; q < NQ; ++q) M[i][NC + DIN + q] = noise_col(i, q);
     }
-    tria<R, DOUT, NCOL>(M);
+    // the noise block is the lower-triangular noise factor unless it is conditional
+    typedef typename std::conditional<COND, PatFull, PatBlocks<DOUT, NC + DIN>>::type Pat;
+    tria_sp<R, DOUT, NCOL, Pat>(M);
     SS_UNROLL
     for (int i = 0; i < DOUT; ++i) {
       SS_UNROLL
@@ -190,7 +192,8 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
       SS_UNROLL
       for (int q = 0; q < NQ; ++q) M[i][NC + 2 * DIN + q] = noise_col(i, q);
     }
-    tria<R, DOUT, NCOL>(M);
+    typedef typename std::conditional<COND, PatFull, PatBlocks<DOUT, NC + 2 * DIN>>::type Pat;
+    tria_sp<R, DOUT, NCOL, Pat>(M);
     SS_UNROLL
     for (int i = 0; i < DOUT; ++i) {
       SS_UNROLL

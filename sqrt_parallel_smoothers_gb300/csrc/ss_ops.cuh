@@ -81,7 +81,7 @@ SS_DEV void filter_element(const Lin<R, NX, NY>& l, const R (&y)[NY], FElem<R, N
     SS_UNROLL
     for (int j = 0; j < NY; ++j) M[NY + r][NX + j] = R(0);
   }
-  tria<R, P, P>(M);
+  tria_sp<R, P, P, PatBlocks<NY, NX>>(M);
   // Psi11 = M[0:NY, 0:NY], Psi21 = M[NY:, 0:NY], U = M[NY:, NY:]
   R W[NY][NX];  // Psi11^{-1} H F
   matmul<R, NY, NX, NX>(l.H, l.F, W);
@@ -140,9 +140,29 @@ SS_DEV void filter_element(const Lin<R, NX, NY>& l, const R (&y)[NY], FElem<R, N
   }
 }
 
+// Zero pattern of xi_core's input [[L^T Z2, I], [Z2, 0]] when only the first
+// ZC columns of Z2 can be non-zero.
+template <int NX, int ZC>
+struct XiPat {
+  __host__ __device__ static constexpr bool nz(int r, int c) {
+    if (r < NX) return c < ZC || c - NX == r;
+    return c < ZC;
+  }
+};
+
+// Zero patterns of a filtering element's Z (filter_element): with NX > NY only
+// its first NY columns are non-zero, otherwise it is lower triangular.  Every
+// combined summary has a lower-triangular Z.  ZK: leading full columns of a Z
+// that is otherwise lower triangular; ZC: columns that can be non-zero.
+template <int NX, int NY>
+struct ElemZ {
+  static constexpr int ZK = NX > NY ? NY : 0;
+  static constexpr int ZC = NX > NY ? NY : NX;
+};
+
 // Xi = tria([[L^T Z2, I], [Z2, 0]]) and V = Xi11^{-1} L^T, the common core of
-// the filtering combine and of its state form.
-template <typename R, int NX>
+// the filtering combine and of its state form.  Columns >= ZC of Z2 are zero.
+template <typename R, int NX, int ZC = NX>
 SS_DEV void xi_core(const R (&L)[NX][NX], const R (&Z2)[NX][NX], R (&X)[2 * NX][2 * NX],
                     R (&V)[NX][NX]) {
   SS_UNROLL
@@ -150,15 +170,17 @@ SS_DEV void xi_core(const R (&L)[NX][NX], const R (&Z2)[NX][NX], R (&X)[2 * NX][
     SS_UNROLL
     for (int j = 0; j < NX; ++j) {
       R s = R(0);
-      SS_UNROLL
-      for (int k = i; k < NX; ++k) s += L[k][i] * Z2[k][j];   // L lower: L[k][i] = 0 for k < i
+      if (j < ZC) {
+        SS_UNROLL
+        for (int k = i; k < NX; ++k) s += L[k][i] * Z2[k][j];   // L lower: L[k][i] = 0 for k < i
+      }
       X[i][j] = s;
       X[i][NX + j] = (i == j) ? R(1) : R(0);
-      X[NX + i][j] = Z2[i][j];
+      X[NX + i][j] = (j < ZC) ? Z2[i][j] : R(0);
       X[NX + i][NX + j] = R(0);
     }
   }
-  tria<R, 2 * NX, 2 * NX>(X);
+  tria_sp<R, 2 * NX, 2 * NX, XiPat<NX, ZC>>(X);
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
@@ -172,11 +194,13 @@ SS_DEV void xi_core(const R (&L)[NX][NX], const R (&Z2)[NX][NX], R (&X)[2 * NX][
 //   A = A2 N, b = A2 (I - V^T Xi21^T)(b1 + U1 U1^T eta2) + b2,
 //   eta = N^T (eta2 - Z2 Z2^T b1) + eta1, U = tria([A2 V^T, U2]),
 //   Z = tria([A1^T Xi22, Z1]).
-template <typename R, int NX>
+// AZK: a.Z is lower triangular apart from its first AZK columns; EZC: only the
+// first EZC columns of e.Z can be non-zero (ElemZ gives both for elements).
+template <typename R, int NX, int AZK = NX, int EZC = NX>
 SS_DEV void filter_combine(FElem<R, NX>& a, const FElem<R, NX>& e) {
   R X[2 * NX][2 * NX];
   R V[NX][NX];
-  xi_core<R, NX>(a.U, e.Z, X, V);
+  xi_core<R, NX, EZC>(a.U, e.Z, X, V);
   // Z = tria([A1^T Xi22, Z1])
   {
     R W[NX][2 * NX];
@@ -191,7 +215,7 @@ SS_DEV void filter_combine(FElem<R, NX>& a, const FElem<R, NX>& e) {
         W[i][NX + j] = a.Z[i][j];
       }
     }
-    tria<R, NX, 2 * NX>(W);
+    tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX, AZK>>(W);
     SS_UNROLL
     for (int i = 0; i < NX; ++i) {
       SS_UNROLL
@@ -280,7 +304,7 @@ SS_DEV void filter_combine(FElem<R, NX>& a, const FElem<R, NX>& e) {
         W[i][NX + j] = e.U[i][j];
       }
     }
-    tria<R, NX, 2 * NX>(W);
+    tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX>>(W);
     SS_UNROLL
     for (int i = 0; i < NX; ++i) {
       SS_UNROLL
@@ -340,7 +364,7 @@ SS_DEV void filter_apply(State<R, NX>& s, const FElem<R, NX>& e) {
       W[i][NX + j] = e.U[i][j];
     }
   }
-  tria<R, NX, 2 * NX>(W);
+  tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX>>(W);
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
@@ -370,7 +394,7 @@ SS_DEV void smoother_element(const R (&F)[NX][NX], const R (&cQ)[NX][NX], const 
       X[NX + i][NX + j] = R(0);
     }
   }
-  tria<R, 2 * NX, 2 * NX>(X);
+  tria_sp<R, 2 * NX, 2 * NX, PatBlocks<NX, NX>>(X);
   // E^T = Phi11^{-T} Phi21^T
   R Et[NX][NX];
   SS_UNROLL
@@ -428,7 +452,7 @@ SS_DEV R filter_update(State<R, NX>& s, const Lin<R, NX, NY>& l, const R (&y)[NY
     SS_UNROLL
     for (int j = 0; j < NY; ++j) M[NY + r][NX + j] = R(0);
   }
-  tria<R, P, P>(M);
+  tria_sp<R, P, P, PatBlocks<NY, NX>>(M);
   R r[NY];
   SS_UNROLL
   for (int k = 0; k < NY; ++k) {
@@ -471,7 +495,7 @@ SS_DEV void smoother_fold(SElem<R, NX>& a, const SElem<R, NX>& e) {
       W[i][NX + j] = a.D[i][j];
     }
   }
-  tria<R, NX, 2 * NX>(W);
+  tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX>>(W);
   R g[NX];
   matvec<R, NX, NX>(a.E, e.g, g);
   R E[NX][NX];
@@ -504,7 +528,7 @@ SS_DEV void smoother_apply(State<R, NX>& s, const SElem<R, NX>& e) {
       W[i][NX + j] = e.D[i][j];
     }
   }
-  tria<R, NX, 2 * NX>(W);
+  tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX>>(W);
   R m[NX];
   matvec<R, NX, NX>(e.E, s.m, m);
   SS_UNROLL

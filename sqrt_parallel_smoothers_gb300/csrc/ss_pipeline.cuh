@@ -49,10 +49,10 @@ SS_DEV void load_lin(const R* p, Lin<R, NX, NY>& l) {
   load_rec<R, Q::LIN>(p, r);
   int o = 0;
   unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  unpack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
+  unpack_lower<R, NX>(r, o, l.cQ); o += NX * NX;
   unpack_vec<R, NX>(r, o, l.bq); o += NX;
   unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  unpack<R, NY, NY>(r, o, l.cR); o += NY * NY;
+  unpack_lower<R, NY>(r, o, l.cR); o += NY * NY;
   unpack_vec<R, NY>(r, o, l.c);
 }
 
@@ -80,7 +80,7 @@ SS_DEV void load_fe(const R* p, FElem<R, NX>& e) {
   int o = 0;
   unpack<R, NX, NX>(r, o, e.A); o += NX * NX;
   unpack_vec<R, NX>(r, o, e.b); o += NX;
-  unpack<R, NX, NX>(r, o, e.U); o += NX * NX;
+  unpack_lower<R, NX>(r, o, e.U); o += NX * NX;
   unpack_vec<R, NX>(r, o, e.eta); o += NX;
   unpack<R, NX, NX>(r, o, e.Z);
 }
@@ -108,7 +108,7 @@ SS_DEV void load_se(const R* p, SElem<R, NX>& e) {
   int o = 0;
   unpack_vec<R, NX>(r, o, e.g); o += NX;
   unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  unpack<R, NX, NX>(r, o, e.D);
+  unpack_lower<R, NX>(r, o, e.D);
 }
 
 template <typename R, int NX>
@@ -130,7 +130,7 @@ SS_DEV void load_st(const R* p, State<R, NX>& s) {
   R r[Q::ST_P];
   load_rec<R, Q::ST>(p, r);
   unpack_vec<R, NX>(r, 0, s.m);
-  unpack<R, NX, NX>(r, NX, s.L);
+  unpack_lower<R, NX>(r, NX, s.L);
 }
 
 template <typename R, int NX>
@@ -260,7 +260,7 @@ SS_DEV void load_noise(const R* qm, const R* qL, R (&m)[D], R (&L)[D][D]) {
   for (int i = 0; i < D; ++i) {
     m[i] = ldg(qm + i);
     SS_UNROLL
-    for (int j = 0; j < D; ++j) L[i][j] = ldg(qL + i * D + j);
+    for (int j = 0; j < D; ++j) L[i][j] = (j <= i) ? ldg(qL + i * D + j) : R(0);   // lower factor
   }
 }
 
@@ -411,7 +411,7 @@ __global__ void __launch_bounds__(128) filter_leaf_kernel(ScanArgs<R> a) {
     } else {
       FElem<R, NX> e;
       filter_element<R, NX, NY>(l, y, e);
-      filter_combine<R, NX>(acc, e);
+      filter_combine<R, NX, ElemZ<NX, NY>::ZK, ElemZ<NX, NY>::ZC>(acc, e);
     }
   }
   store_fe<R, NX>(a.fsum[1] + j * Q::FE_P, acc);

@@ -27,10 +27,10 @@ template <typename R, int NX, int NY>
 SS_DEV void unpack_lin(const R (&r)[Rec<R, NX, NY>::LIN_P], Lin<R, NX, NY>& l) {
   int o = 0;
   unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  unpack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
+  unpack_lower<R, NX>(r, o, l.cQ); o += NX * NX;
   unpack_vec<R, NX>(r, o, l.bq); o += NX;
   unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  unpack<R, NY, NY>(r, o, l.cR); o += NY * NY;
+  unpack_lower<R, NY>(r, o, l.cR); o += NY * NY;
   unpack_vec<R, NY>(r, o, l.c);
 }
 
@@ -50,7 +50,7 @@ SS_DEV void unpack_se(const R (&r)[Rec<R, NX, 1>::SE_P], SElem<R, NX>& e) {
   int o = 0;
   unpack_vec<R, NX>(r, o, e.g); o += NX;
   unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  unpack<R, NX, NX>(r, o, e.D);
+  unpack_lower<R, NX>(r, o, e.D);
 }
 
 constexpr int STAGED_BLOCK = 128;
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_leaf_staged
       } else {
         FElem<R, NX> e;
         filter_element<R, NX, NY>(l, y, e);
-        filter_combine<R, NX>(acc, e);
+        filter_combine<R, NX, ElemZ<NX, NY>::ZK, ElemZ<NX, NY>::ZC>(acc, e);
       }
     }
     __syncwarp();
@@ -215,29 +215,50 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    R srec[Q::SE_P];
-    SS_UNROLL
-    for (int q = 0; q < Q::SE_P; ++q) srec[q] = R(0);
+    // Order within a step keeps the live set small: the smoothing element is
+    // staged out first, then the Kalman update consumes the predicted factor,
+    // and the fold into the chunk summary runs last.
+    // The record parts and the element are re-read from shared memory where
+    // they are used again (the fences keep the compiler from holding the first
+    // reads in registers).
+    const R* tile = tiles + (k & 1) * TL::WARP_ELEMS;
+    R X[2 * NX][2 * NX], mp[NX];
+    {
+      R srec[Q::SE_P];
+      SS_UNROLL
+      for (int q = 0; q < Q::SE_P; ++q) srec[q] = R(0);
+      if (k < n) {
+        R rec[Q::LIN_P];
+        stage_read<R, Q::LIN>(tile, rec);
+        Lin<R, NX, NY> l;
+        unpack_lin<R, NX, NY>(rec, l);
+        SElem<R, NX> se;
+        smoother_element<R, NX>(l.F, l.cQ, l.bq, s, se, X, mp);
+        if (a.emit_smoother) pack_se<R, NX>(srec, se);
+      }
+      if (a.emit_smoother)
+        stage_store<R, Q::SE>(stile, srec, k < n ? a.selem + (first + k) * Q::SE_P : nullptr);
+    }
     if (k < n) {
+      compiler_fence();
       R rec[Q::LIN_P];
-      stage_read<R, Q::LIN>(tiles + (k & 1) * TL::WARP_ELEMS, rec);
+      stage_read<R, Q::LIN>(tile, rec);
       Lin<R, NX, NY> l;
       unpack_lin<R, NX, NY>(rec, l);
       R y[NY];
       SS_UNROLL
       for (int q = 0; q < NY; ++q) y[q] = a.ys[(first + k) * NY + q];
-      R X[2 * NX][2 * NX], mp[NX];
-      SElem<R, NX> se;
-      smoother_element<R, NX>(l.F, l.cQ, l.bq, s, se, X, mp);
-      if (a.emit_smoother) {
-        pack_se<R, NX>(srec, se);
-        if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
-      }
       ll += (double)filter_update<R, NX, NY>(s, l, y, X, mp);
       if (a.filt_m != nullptr) store_traj<R, NX>(a.filt_m, a.filt_L, first + i + k + 1, s);
     }
-    if (a.emit_smoother)
-      stage_store<R, Q::SE>(stile, srec, k < n ? a.selem + (first + k) * Q::SE_P : nullptr);
+    if (k < n && a.emit_smoother) {
+      compiler_fence();
+      R rec[Q::SE_P];
+      stage_read<R, Q::SE>(stile, rec);   // this lane's row still holds its element
+      SElem<R, NX> se;
+      unpack_se<R, NX>(rec, se);
+      if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
+    }
     __syncwarp();
   }
   cp_async_wait<0>();

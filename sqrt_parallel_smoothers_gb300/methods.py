@@ -704,9 +704,9 @@ def iterated_smoothing(observations, x0, transition_model, observation_model, li
                                  _std_to_sqrt(init_nominal_trajectory), parallel, criterion, return_loglikelihood,
                                  lengths=lengths, offsets=offsets, chunk=chunk, group=group, slr_form=slr_form,
                                  return_info=return_info)
-        if isinstance(out, tuple):
-            return (_sqrt_to_std(out[0]),) + tuple(out[1:])
-        return _sqrt_to_std(out)
+        if isinstance(out, MVNSqrt):   # MVNSqrt is itself a tuple: test it first
+            return _sqrt_to_std(out)
+        return (_sqrt_to_std(out[0]),) + tuple(out[1:])
     method = _check_common(x0, parallel, linearization_method)
     if init_nominal_trajectory is not None:
         are_inputs_compatible(x0, init_nominal_trajectory)
