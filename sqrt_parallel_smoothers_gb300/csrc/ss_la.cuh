@@ -21,6 +21,13 @@ SS_DEV double ss_log(double x) { return log(x); }
 SS_DEV bool ss_isfinite(float x) { return isfinite(x); }
 SS_DEV bool ss_isfinite(double x) { return isfinite(x); }
 
+// Correctly rounded reciprocal (the triangular solves' pivots); other scalar
+// types (dual numbers) use their division.
+SS_DEV float ss_rcp(float x) { return __frcp_rn(x); }
+SS_DEV double ss_rcp(double x) { return __drcp_rn(x); }
+template <typename R>
+SS_DEV R ss_rcp(const R& x) { return R(1) / x; }
+
 // ---------------------------------------------------------------------------
 // tria: on return M[:, :ROWS] holds the lower-triangular L (diag >= 0) with
 // L L^T = M M^T (input M), and M[:, ROWS:] is zero.  Householder reflections
@@ -87,10 +94,10 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
 // touches, so the pattern of every intermediate matrix follows from the input
 // pattern alone.  TriaPlan runs that propagation at compile time: for each
 // reflector i, the columns > i it carries (sup) and the rows > i it changes
-// (touch).  The device loop then skips products with structural zeros.  The
-// skipped terms are exact zeros in tria's arithmetic (0 * v added to a partial
-// sum, a row updated by w = 0), and the partial sums alternate on the same
-// column parity, so the result equals tria's on finite inputs.
+// (touch).  The device loop then skips products with structural zeros (exact
+// zeros in tria's arithmetic).  Each reflector is applied in the unscaled form
+// H = I + u u^T / (beta v0), one reciprocal per reflector, so the result equals
+// tria's up to rounding.
 //
 // PAT::nz(r, c) is true where the input may be non-zero; entries it calls zero
 // are taken as zero.
@@ -163,31 +170,28 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
       const R sigma = sig0 + sig1;
       const R x0 = M[i][i];
       if (sigma != R(0)) {
+        // H = I + u u^T / (beta v0), u = (v0, M[i][i+1:]), v0 = x0 - beta:
+        // one reciprocal per reflector, no scaled copy of the row.
         const R nrm = ss_sqrt(x0 * x0 + sigma);
-        beta = (x0 <= R(0)) ? nrm : -nrm;
+        beta = (x0 <= R(0)) ? nrm : -nrm;   // opposite sign of x0: no cancellation in v0
         const R v0 = x0 - beta;
-        const R tau = -v0 / beta;
-        const R inv = R(1) / v0;
-        R v[COLS];
-        SS_UNROLL
-        for (int j = i + 1; j < COLS; ++j)
-          if ((SUP >> j) & 1) v[j] = M[i][j] * inv;
+        const R k = R(1) / (beta * v0);
         SS_UNROLL
         for (int r = i + 1; r < ROWS; ++r) {
           if ((TOUCH >> r) & 1) {
-            R w0 = M[r][i], w1 = R(0);
+            R d0 = M[r][i] * v0, d1 = R(0);
             SS_UNROLL
             for (int j = i + 1; j < COLS; ++j) {
               if ((SUP >> j) & 1) {
-                if ((j - i) & 1) w1 += M[r][j] * v[j];
-                else w0 += M[r][j] * v[j];
+                if ((j - i) & 1) d1 += M[r][j] * M[i][j];
+                else d0 += M[r][j] * M[i][j];
               }
             }
-            const R w = (w0 + w1) * tau;
-            M[r][i] -= w;
+            const R c = (d0 + d1) * k;
+            M[r][i] += c * v0;
             SS_UNROLL
             for (int j = i + 1; j < COLS; ++j)
-              if ((SUP >> j) & 1) M[r][j] -= w * v[j];
+              if ((SUP >> j) & 1) M[r][j] += c * M[i][j];
           }
         }
       }
@@ -227,7 +231,7 @@ template <typename R, int N, int K, int R0 = 0, int C0 = 0, int MR, int MC>
 SS_DEV void solve_lower(const R (&M)[MR][MC], R (&B)[N][K]) {
   SS_UNROLL
   for (int i = 0; i < N; ++i) {
-    const R inv = R(1) / M[R0 + i][C0 + i];
+    const R inv = ss_rcp(M[R0 + i][C0 + i]);
     SS_UNROLL
     for (int k = 0; k < K; ++k) {
       R s = B[i][k];
@@ -246,7 +250,7 @@ SS_DEV void solve_lower_vec(const R (&M)[MR][MC], R (&b)[N]) {
     R s = b[i];
     SS_UNROLL
     for (int j = 0; j < i; ++j) s -= M[R0 + i][C0 + j] * b[j];
-    b[i] = s / M[R0 + i][C0 + i];
+    b[i] = s * ss_rcp(M[R0 + i][C0 + i]);
   }
 }
 
@@ -255,7 +259,7 @@ template <typename R, int N, int K, int R0 = 0, int C0 = 0, int MR, int MC>
 SS_DEV void solve_lower_T(const R (&M)[MR][MC], R (&B)[N][K]) {
   SS_UNROLL
   for (int i = N - 1; i >= 0; --i) {
-    const R inv = R(1) / M[R0 + i][C0 + i];
+    const R inv = ss_rcp(M[R0 + i][C0 + i]);
     SS_UNROLL
     for (int k = 0; k < K; ++k) {
       R s = B[i][k];

@@ -21,6 +21,16 @@ template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_sin(const Dual<T, NT>& a) { return chain(a, ss_sin(a.v), ss_cos(a.v)); }
 template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_cos(const Dual<T, NT>& a) { return chain(a, ss_cos(a.v), -ss_sin(a.v)); }
+// sin and cos of one angle with one range reduction.
+SS_DEV void ss_sincos(float x, float& s, float& c) { sincosf(x, &s, &c); }
+SS_DEV void ss_sincos(double x, double& s, double& c) { sincos(x, &s, &c); }
+template <typename T, int NT>
+SS_DEV void ss_sincos(const Dual<T, NT>& a, Dual<T, NT>& s, Dual<T, NT>& c) {
+  T sv, cv;
+  ss_sincos(a.v, sv, cv);
+  s = chain(a, sv, cv);
+  c = chain(a, cv, -sv);
+}
 template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_atan2(const Dual<T, NT>& y, const Dual<T, NT>& x) {
   Dual<T, NT> r;
@@ -79,14 +89,14 @@ struct CoordinatedTurnFn {
   R dt;
   SS_DEV void init(const ModelArgs<R>& a) { dt = a.p[0]; }
   SS_DEV void coeffs(R w, R& c, R& s, R& sw, R& cw) const {
-    c = ss_cos(w * dt);
-    s = ss_sin(w * dt);
+    ss_sincos(w * dt, s, c);
     if (ss_abs(w) < R(1e-6)) {
       sw = dt;
       cw = R(0);
     } else {
-      sw = s / w;
-      cw = (c - R(1)) / w;
+      const R iw = ss_rcp(w);
+      sw = s * iw;
+      cw = (c - R(1)) * iw;
     }
   }
   SS_DEV void eval(const R (&x)[DIN], R (&y)[DOUT]) const {
@@ -104,8 +114,9 @@ struct CoordinatedTurnFn {
     coeffs(w, c, s, sw, cw);
     R dsw = R(0), dcw = R(0);
     if (!(ss_abs(w) < R(1e-6))) {
-      dsw = dt * c / w - s / (w * w);
-      dcw = -dt * s / w - (c - R(1)) / (w * w);
+      const R iw = ss_rcp(w);
+      dsw = (dt * c - sw) * iw;
+      dcw = (-dt * s - cw) * iw;
     }
     SS_UNROLL
     for (int i = 0; i < 5; ++i) {

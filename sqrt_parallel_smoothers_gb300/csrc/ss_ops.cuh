@@ -315,6 +315,120 @@ SS_DEV void filter_combine(FElem<R, NX>& a, const FElem<R, NX>& e) {
   matmul<R, NX, NX, NX>(e.A, N, a.A);
 }
 
+// Zero pattern of [Z, W^T] in filter_extend: Z lower triangular apart from its
+// first ZK columns, W^T (NX x NY) full.
+template <int NX, int ZK>
+struct ZExtPat {
+  __host__ __device__ static constexpr bool nz(int r, int c) { return c >= NX || c <= r || c < ZK; }
+};
+
+// a <- a (x) filter_element(l, y), computed without the element: the summary
+// of a chunk's steps, x_t | x_s ~ N(A x_s + b, U U^T) with information
+// (eta, Z Z^T) on the state x_s before the chunk, extended by one Kalman step
+// in conditional form.  Predict: Ap = F A, bp = F b + bq, Up = tria([F U, cQ]);
+// update with y = H x + c + N(0, cR cR^T): tria([[H Up, cR], [Up, 0]]) gives
+// Psi11 (innovation factor), Psi21 and U' = Psi22, and with
+// W = Psi11^{-1} H Ap and r = Psi11^{-1} (y - H bp - c):
+//   A' = Ap - Psi21 W,  b' = bp + Psi21 r,  eta' = eta + W^T r,
+//   Z' = tria([Z, W^T]).
+// The result is the associative combine of parsmooth/parallel/_operators.py:43-77
+// applied to the element of parsmooth/parallel/_filtering.py:115-146 (the same
+// conditional distribution and information), at about half its arithmetic.
+// AZK: a.Z is lower triangular apart from its first AZK columns.
+template <typename R, int NX, int NY, int AZK = NX>
+SS_DEV void filter_extend(FElem<R, NX>& a, const Lin<R, NX, NY>& l, const R (&y)[NY]) {
+  constexpr int P = NX + NY;
+  R M[P][P];
+  {
+    R X[NX][2 * NX];
+    SS_UNROLL
+    for (int i = 0; i < NX; ++i) {
+      SS_UNROLL
+      for (int j = 0; j < NX; ++j) {
+        R q = R(0);
+        SS_UNROLL
+        for (int k = j; k < NX; ++k) q += l.F[i][k] * a.U[k][j];
+        X[i][j] = q;
+        X[i][NX + j] = l.cQ[i][j];
+      }
+    }
+    tria_sp<R, NX, 2 * NX, PatBlocks<NX, NX>>(X);
+    SS_UNROLL
+    for (int r = 0; r < NY; ++r) {
+      SS_UNROLL
+      for (int j = 0; j < NX; ++j) {
+        R q = R(0);
+        SS_UNROLL
+        for (int k = j; k < NX; ++k) q += l.H[r][k] * X[k][j];
+        M[r][j] = q;
+      }
+      SS_UNROLL
+      for (int j = 0; j < NY; ++j) M[r][NX + j] = l.cR[r][j];
+    }
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      SS_UNROLL
+      for (int j = 0; j < NX; ++j) M[NY + r][j] = X[r][j];
+      SS_UNROLL
+      for (int j = 0; j < NY; ++j) M[NY + r][NX + j] = R(0);
+    }
+  }
+  tria_sp<R, P, P, PatBlocks<NY, NX>>(M);
+  R Ap[NX][NX], bp[NX];
+  matmul<R, NX, NX, NX>(l.F, a.A, Ap);
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    R q = l.bq[i];
+    SS_UNROLL
+    for (int k = 0; k < NX; ++k) q += l.F[i][k] * a.b[k];
+    bp[i] = q;
+  }
+  R W[NY][NX], r[NY];
+  matmul<R, NY, NX, NX>(l.H, Ap, W);
+  solve_lower<R, NY, NX>(M, W);
+  SS_UNROLL
+  for (int k = 0; k < NY; ++k) {
+    R q = y[k] - l.c[k];
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) q -= l.H[k][j] * bp[j];
+    r[k] = q;
+  }
+  solve_lower_vec<R, NY>(M, r);
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    R q = bp[i], e = a.eta[i];
+    SS_UNROLL
+    for (int k = 0; k < NY; ++k) {
+      q += M[NY + i][k] * r[k];
+      e += W[k][i] * r[k];
+    }
+    a.b[i] = q;
+    a.eta[i] = e;
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) {
+      R s = Ap[i][j];
+      SS_UNROLL
+      for (int k = 0; k < NY; ++k) s -= M[NY + i][k] * W[k][j];
+      a.A[i][j] = s;
+      a.U[i][j] = (j <= i) ? M[NY + i][NY + j] : R(0);
+    }
+  }
+  R Zx[NX][NX + NY];
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) Zx[i][j] = a.Z[i][j];
+    SS_UNROLL
+    for (int k = 0; k < NY; ++k) Zx[i][NX + k] = W[k][i];
+  }
+  tria_sp<R, NX, NX + NY, ZExtPat<NX, AZK>>(Zx);
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) a.Z[i][j] = (j <= i) ? Zx[i][j] : R(0);
+  }
+}
+
 // State form of the filtering combine: (m, L) <- combine((., m, L, ., .), e)
 // restricted to its (b, U) outputs.
 template <typename R, int NX>

@@ -409,9 +409,7 @@ __global__ void __launch_bounds__(128) filter_leaf_kernel(ScanArgs<R> a) {
     if (t == t0) {
       filter_element<R, NX, NY>(l, y, acc);
     } else {
-      FElem<R, NX> e;
-      filter_element<R, NX, NY>(l, y, e);
-      filter_combine<R, NX, ElemZ<NX, NY>::ZK, ElemZ<NX, NY>::ZC>(acc, e);
+      filter_extend<R, NX, NY, ElemZ<NX, NY>::ZK>(acc, l, y);
     }
   }
   store_fe<R, NX>(a.fsum[1] + j * Q::FE_P, acc);

@@ -69,6 +69,23 @@ inline int make_layout(const ss_problem& p, Layout& y) {
   const int64_t B = p.batch, N = p.total_steps;
   y.C = p.chunk > 0 ? p.chunk : 16;
   y.G = p.group > 1 ? p.group : 8;
+  if (p.chunk <= 0 && p.group <= 1) {
+    // Automatic geometry.  A problem whose level-1 chunks fit in one wave of
+    // resident threads (152 SMs x 256 threads at the chunk kernels' register
+    // use) is latency-bound: the time is the chain one thread walks (C steps at
+    // the leaf, G summaries per level, up to 4G at the top), so the smallest
+    // chunk that still fits one wave, with G = 4, is the shortest chain.
+    constexpr int64_t ONE_WAVE = 152 * 256;
+    for (int c : {4, 8}) {
+      if (N / c + B <= ONE_WAVE) {
+        int64_t n = (p.max_len + c - 1) / c;
+        int levels = 1;
+        while (n > 16) { n = (n + 3) / 4; ++levels; }
+        if (levels <= MAX_LEVELS) { y.C = c; y.G = 4; }
+        break;
+      }
+    }
+  }
   const int64_t top = 4 * (int64_t)y.G;
   int64_t n = (p.max_len + y.C - 1) / y.C;
   y.L = 1;

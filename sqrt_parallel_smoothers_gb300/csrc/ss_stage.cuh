@@ -30,9 +30,6 @@ SS_DEV void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-// Compiler-only memory fence: values read from shared memory before it are
-// read again after it instead of being kept in registers.
-SS_DEV void compiler_fence() { asm volatile("" ::: "memory"); }
 SS_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 SS_DEV void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }

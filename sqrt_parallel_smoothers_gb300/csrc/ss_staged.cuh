@@ -172,9 +172,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_leaf_staged
       if (s == 0) {
         filter_element<R, NX, NY>(l, y, acc);
       } else {
-        FElem<R, NX> e;
-        filter_element<R, NX, NY>(l, y, e);
-        filter_combine<R, NX, ElemZ<NX, NY>::ZK, ElemZ<NX, NY>::ZC>(acc, e);
+        filter_extend<R, NX, NY, ElemZ<NX, NY>::ZK>(acc, l, y);
       }
     }
     __syncwarp();
@@ -215,14 +213,12 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
     cp_async_commit();
     cp_async_wait<1>();
     __syncwarp();
-    // Order within a step keeps the live set small: the smoothing element is
-    // staged out first, then the Kalman update consumes the predicted factor,
-    // and the fold into the chunk summary runs last.
-    // The record parts and the element are re-read from shared memory where
-    // they are used again (the fences keep the compiler from holding the first
-    // reads in registers).
+    // Order within a step, chosen by measurement: the smoothing element is
+    // staged out and folded while the predicted factor waits, then the record's
+    // observation part is read again from shared memory for the Kalman update.
     const R* tile = tiles + (k & 1) * TL::WARP_ELEMS;
     R X[2 * NX][2 * NX], mp[NX];
+    SElem<R, NX> se;
     {
       R srec[Q::SE_P];
       SS_UNROLL
@@ -232,15 +228,16 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
         stage_read<R, Q::LIN>(tile, rec);
         Lin<R, NX, NY> l;
         unpack_lin<R, NX, NY>(rec, l);
-        SElem<R, NX> se;
         smoother_element<R, NX>(l.F, l.cQ, l.bq, s, se, X, mp);
         if (a.emit_smoother) pack_se<R, NX>(srec, se);
       }
       if (a.emit_smoother)
         stage_store<R, Q::SE>(stile, srec, k < n ? a.selem + (first + k) * Q::SE_P : nullptr);
     }
+    if (k < n && a.emit_smoother) {
+      if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
+    }
     if (k < n) {
-      compiler_fence();
       R rec[Q::LIN_P];
       stage_read<R, Q::LIN>(tile, rec);
       Lin<R, NX, NY> l;
@@ -250,14 +247,6 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
       for (int q = 0; q < NY; ++q) y[q] = a.ys[(first + k) * NY + q];
       ll += (double)filter_update<R, NX, NY>(s, l, y, X, mp);
       if (a.filt_m != nullptr) store_traj<R, NX>(a.filt_m, a.filt_L, first + i + k + 1, s);
-    }
-    if (k < n && a.emit_smoother) {
-      compiler_fence();
-      R rec[Q::SE_P];
-      stage_read<R, Q::SE>(stile, rec);   // this lane's row still holds its element
-      SElem<R, NX> se;
-      unpack_se<R, NX>(rec, se);
-      if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
     }
     __syncwarp();
   }

@@ -800,11 +800,19 @@ class IteratedSmootherPlan:
     ``(sum (T_i+1), nx)`` layout) and :attr:`ell` (when requested).  With
     ``profile=True`` every captured kernel is bracketed by CUDA events that
     each replay re-records; ``_lib.profile_read()`` returns the last replay's
-    per-kernel times (call ``_lib.profile_reset()`` only after the plan is gone)."""
+    per-kernel times (call ``_lib.profile_reset()`` only after the plan is gone).
+
+    ``streams=k`` (k > 1, with ``graph=True``) cuts the batch into k contiguous
+    groups of sequences with about equal step counts and captures each group's
+    loop on its own stream of the same graph: the groups are independent, so
+    one group's per-step kernels fill the GPU while another is in its scan
+    levels (a few hundred threads each).  Each group has its own workspace and
+    writes its slice of the shared outputs."""
 
     def __init__(self, observations, x0, transition_model, observation_model, linearization_method,
                  init_nominal_trajectory=None, criterion=_default_criterion, return_loglikelihood=False, *,
-                 lengths=None, offsets=None, chunk=0, group=0, slr_form=0, graph=True, profile=False):
+                 lengths=None, offsets=None, chunk=0, group=0, slr_form=0, graph=True, profile=False,
+                 streams=1):
         method = _check_common(x0, True, linearization_method)
         if init_nominal_trajectory is not None:
             are_inputs_compatible(x0, init_nominal_trajectory)
@@ -823,6 +831,9 @@ class IteratedSmootherPlan:
         self._args = (lay.ys, lay.offsets, m0, L0, im, iL, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg)
         self.steps = lay.N
         self.graph = None
+        if graph and streams > 1 and lay.B > 1:
+            self._build_grouped(int(streams), profile)
+            return
         stream = torch.cuda.Stream(dev)
         stream.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(stream):
@@ -843,6 +854,79 @@ class IteratedSmootherPlan:
                     if profile:
                         _lib.profile_enable(False)
                 self.graph = g
+        torch.cuda.current_stream(dev).wait_stream(stream)
+        torch.cuda.synchronize(dev)
+
+    def _build_grouped(self, k, profile):
+        """Concurrent sequence groups (see the class docstring)."""
+        (ys, offsets, m0, L0, im, iL, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg) = self._args
+        lay, nx, dev = self.layout, self.nx, ys.device
+        off = np.concatenate([[0], np.cumsum(lay.lengths)]).astype(np.int64)
+        k = min(k, lay.B)
+        cuts = [0]
+        for g in range(1, k):          # about equal steps per group, no group empty
+            c = int(np.searchsorted(off, g * off[-1] / k))
+            cuts.append(max(cuts[-1] + 1, min(c, lay.B - (k - g))))
+        cuts.append(lay.B)
+        cuts = [c for i, c in enumerate(cuts) if i == 0 or off[c] > off[cuts[i - 1]] or c == lay.B]
+        if len(cuts) > 2 and off[cuts[-1]] == off[cuts[-2]]:
+            del cuts[-2]                 # every group holds at least one step
+        per, want_ell, n_iter, tol = icfg[13], icfg[14], icfg[15], fcfg[11]
+        N, B = lay.N, lay.B
+        out_m = torch.empty((N + B, nx), dtype=ys.dtype, device=dev)
+        out_L = torch.empty((N + B, nx, nx), dtype=ys.dtype, device=dev)
+        ell = torch.empty((B if want_ell else 0,), dtype=torch.float64, device=dev)
+        iters = torch.empty((B,), dtype=torch.int32, device=dev)
+        flags = torch.empty((B,), dtype=torch.int32, device=dev)
+        self._outs = (out_m, out_L, ell, iters, flags)
+        lib = _lib.load()
+        calls = []
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            s0, s1 = int(off[a]) + a, int(off[b]) + b          # state rows of the group
+            lens = lay.lengths[a:b]
+            og = torch.as_tensor(off[a:b + 1] - off[a], dtype=torch.int64, device=dev)
+            cfg = list(icfg)
+            cfg[10], cfg[11], cfg[12] = b - a, int(lens.sum()), int(lens.max())
+            pr = _problem(cfg, fcfg, ys.dtype, og, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+            nbytes = _lib.ctypes.c_size_t(0)
+            _lib.check(lib.ss_workspace_bytes(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
+            ws = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=dev)
+            gm0, gL0 = (m0[a:b], L0[a:b]) if per else (m0, L0)
+            gim, giL = (im[s0:s1], iL[s0:s1]) if im is not None else (None, None)
+            calls.append(dict(pr=pr, og=og, ws=ws, nbytes=nbytes.value, ys=ys[int(off[a]):int(off[b])],
+                              m0=gm0, L0=gL0, im=gim, iL=giL, m=out_m[s0:s1], L=out_L[s0:s1],
+                              ell=ell[a:b] if want_ell else None, iters=iters[a:b], flags=flags[a:b],
+                              stream=torch.cuda.Stream(dev)))
+        self._groups = calls
+
+        def launch(main):
+            for c in calls:
+                c["stream"].wait_stream(main)
+                _lib.check(lib.ss_iterated(_lib.ctypes.byref(c["pr"]), _ptr(c["ys"]), _ptr(c["m0"]), _ptr(c["L0"]),
+                                           per, _ptr(c["im"]), _ptr(c["iL"]), n_iter, tol, _ptr(c["m"]),
+                                           _ptr(c["L"]), _ptr(c["ell"]), _ptr(c["iters"]), _ptr(c["flags"]),
+                                           _ptr(c["ws"]), c["nbytes"], c["stream"].cuda_stream))
+            for c in calls:
+                main.wait_stream(c["stream"])
+
+        stream = torch.cuda.Stream(dev)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(stream):
+            launch(stream)                      # warm-up
+            n0 = _lib.launch_count()
+            launch(stream)
+            self.launches_per_run = _lib.launch_count() - n0
+            g = torch.cuda.CUDAGraph()
+            if profile:
+                _lib.profile_reset()
+                _lib.profile_enable(True)
+            try:
+                with torch.cuda.graph(g, stream=stream):
+                    launch(stream)
+            finally:
+                if profile:
+                    _lib.profile_enable(False)
+            self.graph = g
         torch.cuda.current_stream(dev).wait_stream(stream)
         torch.cuda.synchronize(dev)
 

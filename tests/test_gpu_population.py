@@ -45,16 +45,17 @@ def test_population_linearize(method):
 @pytest.mark.parametrize("method", ["extended", "cubature"])
 @pytest.mark.parametrize("sqrt", [True, False])
 def test_population_iterated_vs_oracle(method, sqrt):
-    """The reference's population experiment: T = 128, random prior and nominal (the
-    notebook's), 10 iterations, FP64."""
+    """The reference's population workload (T = 128, 10 iterations, FP64) from a
+    well-conditioned start: the nominal means log((y + 1) / lam) read off the counts.  From a
+    random nominal, undamped Gauss-Newton on this chaotic map leaves the data's basin (the
+    oracle itself overflows within three iterations), and rounding differences then grow
+    without bound, so such a start says nothing about parity."""
     T = 128
     _, ys = S.data.population_data(T)
-    rng = np.random.RandomState(0)
-    m0 = rng.randn(1)
-    c0 = rng.randn(1, 1)
-    P0 = c0 @ c0.T
-    m_nom = rng.randn(T + 1, 1)
-    P_nom = np.repeat(np.eye(1)[None], T + 1, 0)
+    m0 = np.array([np.log(7.0)])
+    P0 = np.array([[0.25]])
+    m_nom = np.concatenate([m0[None], np.log((ys + 1.0) / LAM)], 0)
+    P_nom = np.repeat(0.5 * np.eye(1)[None], T + 1, 0)
     of, oh = _oracle_models(sqrt)
     gf, gh = _gpu_models(sqrt)
     if sqrt:
