@@ -546,10 +546,10 @@ def gpu_arm(args):
     tuning = None
     if args.chunk == 0 and not args.no_autotune:
         from sqrt_parallel_smoothers_gb300 import autotune
-        key = autotune.signature(5, 2, "f32", lengths, "cubature")
-        args.chunk, args.group, tuning = autotune.tune(
-            lambda c, g: make_plan(torch, S, batch["ys"], offsets, torch.float32, c, g), key=key)
-    plan = make_plan(torch, S, batch["ys"], offsets, torch.float32, args.chunk, args.group)
+        key = autotune.signature(5, 2, "f32", lengths, "cubature") + ":streams"
+        (args.chunk, args.group, args.streams), tuning = autotune.tune(
+            lambda c, g, k: make_plan(torch, S, batch["ys"], offsets, torch.float32, c, g, streams=k), key=key)
+    plan = make_plan(torch, S, batch["ys"], offsets, torch.float32, args.chunk, args.group, streams=args.streams)
     C = args.chunk or 16
     G = args.group or 8
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
@@ -587,7 +587,8 @@ def gpu_arm(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded simulator of the reference's "
                                                        "bearings experiment)",
-            "config": workload_config(args.batch, lengths, C, G), "e2e": e2e, "gpu_launches": int(launches),
+            "config": dict(workload_config(args.batch, lengths, C, G), streams=int(args.streams)), "e2e": e2e,
+            "gpu_launches": int(launches),
             "clocks": clocks}
     if tuning is not None:
         line["config"]["autotune_ms"] = tuning
@@ -696,6 +697,7 @@ def main():
     ap.add_argument("--batch", type=int, default=B_DEFAULT)
     ap.add_argument("--chunk", type=int, default=0)
     ap.add_argument("--group", type=int, default=0)
+    ap.add_argument("--streams", type=int, default=1, help="concurrent sequence groups (tuned with --chunk 0)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-main", action="store_true", help="time the FP32 batched smoother and its kernels only")
     ap.add_argument("--no-autotune", action="store_true", help="use the default chunk/group (16, 8)")

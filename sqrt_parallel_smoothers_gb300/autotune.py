@@ -1,4 +1,5 @@
-"""Autotuner for the scan geometry (steps per chunk C, summaries per group G).
+"""Autotuner for the scan geometry (steps per chunk C, summaries per group G) and the
+number of concurrent sequence groups S.
 
 The chunk kernels are register-bound (one thread holds a chunk's square-root
 summary), so C trades resident-thread waves on the 152 SMs against the work
@@ -12,8 +13,9 @@ import os
 
 import torch
 
-DEFAULT_CANDIDATES = ((8, 8), (16, 8), (16, 4), (24, 4), (24, 8), (32, 2), (32, 4), (32, 8), (48, 4), (48, 8),
-                      (64, 4), (64, 8))
+# (steps per chunk C, summaries per group G, concurrent sequence groups S)
+DEFAULT_CANDIDATES = ((8, 8, 1), (16, 8, 1), (16, 4, 1), (32, 2, 1), (32, 4, 1), (32, 8, 1), (48, 4, 1),
+                      (16, 4, 2), (16, 4, 4), (24, 4, 4), (32, 4, 2), (32, 4, 3), (16, 8, 4), (8, 8, 4))
 
 
 def cache_path():
@@ -64,23 +66,22 @@ def time_plan(plan, reps=5):
 
 
 def tune(make_plan, key=None, candidates=DEFAULT_CANDIDATES, reps=5, use_cache=True):
-    """Pick ``(chunk, group)`` for ``make_plan(chunk, group) -> IteratedSmootherPlan``.
+    """Pick a geometry for ``make_plan(*candidate) -> IteratedSmootherPlan``.
 
-    Returns ``(chunk, group, {"C,G": ms})``; with a ``key`` the result is cached."""
+    Candidates are tuples such as ``(chunk, group, streams)``.  Returns
+    ``(best_candidate, {"C,G,S": ms})``; with a ``key`` the result is cached."""
     table = _load() if (use_cache and key) else {}
     if key and key in table:
-        c, g = table[key]["best"]
-        return c, g, table[key]["ms"]
+        return tuple(table[key]["best"]), table[key]["ms"]
     results = {}
-    for c, g in candidates:
-        plan = make_plan(c, g)
-        results[f"{c},{g}"] = time_plan(plan, reps)
+    for cand in candidates:
+        plan = make_plan(*cand)
+        results[",".join(str(v) for v in cand)] = time_plan(plan, reps)
         del plan
         torch.cuda.empty_cache()
-    best = min(results, key=results.get)
-    c, g = (int(v) for v in best.split(","))
+    best = tuple(int(v) for v in min(results, key=results.get).split(","))
     if key:
         table = _load()
-        table[key] = {"best": [c, g], "ms": results}
+        table[key] = {"best": list(best), "ms": results}
         _store(table)
-    return c, g, results
+    return best, results
