@@ -461,15 +461,23 @@ SS_DEV void unpack(const R (&rec)[P], int off, R (&A)[M][N]) {
     for (int j = 0; j < N; ++j) A[i][j] = rec[off + i * N + j];
   }
 }
-// Lower-triangular factor stored as a full square: the upper entries are
-// zero by construction, and setting them here lets the compiler treat them as
-// constants.
+// Lower-triangular factor stored as its N (N + 1) / 2 lower entries, row by
+// row; unpacking sets the upper entries to zero, so the compiler treats them
+// as constants.
 template <typename R, int N, int P>
-SS_DEV void unpack_lower(const R (&rec)[P], int off, R (&A)[N][N]) {
+SS_DEV void pack_tri(R (&rec)[P], int off, const R (&A)[N][N]) {
   SS_UNROLL
   for (int i = 0; i < N; ++i) {
     SS_UNROLL
-    for (int j = 0; j < N; ++j) A[i][j] = (j <= i) ? rec[off + i * N + j] : R(0);
+    for (int j = 0; j <= i; ++j) rec[off + i * (i + 1) / 2 + j] = A[i][j];
+  }
+}
+template <typename R, int N, int P>
+SS_DEV void unpack_tri(const R (&rec)[P], int off, R (&A)[N][N]) {
+  SS_UNROLL
+  for (int i = 0; i < N; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < N; ++j) A[i][j] = (j <= i) ? rec[off + i * (i + 1) / 2 + j] : R(0);
   }
 }
 template <typename R, int N, int P>

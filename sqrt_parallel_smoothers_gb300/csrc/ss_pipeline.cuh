@@ -28,47 +28,62 @@ namespace ss {
 
 constexpr int MAX_LEVELS = 8;
 
+// Record sizes (elements; _P: padded to whole 16-byte units).  Lower-triangular
+// factors are stored as their lower entries only (pack_tri).
 template <typename R, int NX, int NY>
 struct Rec {
-  static constexpr int LIN = 2 * NX * NX + NX + NY * NX + NY * NY + NY;
+  static constexpr int TX = NX * (NX + 1) / 2, TY = NY * (NY + 1) / 2;
+  static constexpr int LIN = NX * NX + TX + NX + NY * NX + TY + NY;   // F, cQ, bq, H, cR, c
   static constexpr int LIN_P = Padded<R, LIN>::n;
-  static constexpr int FE = 3 * NX * NX + 2 * NX;
+  static constexpr int FE = 2 * NX * NX + TX + 2 * NX;                 // A, b, U, eta, Z
   static constexpr int FE_P = Padded<R, FE>::n;
-  static constexpr int SE = NX + 2 * NX * NX;
+  static constexpr int SE = NX + NX * NX + TX;                         // g, E, D
   static constexpr int SE_P = Padded<R, SE>::n;
-  static constexpr int ST = NX + NX * NX;
+  static constexpr int ST = NX + TX;                                   // m, L
   static constexpr int ST_P = Padded<R, ST>::n;
 };
 
 // ----------------------------------------------------------------------------- records
 
 template <typename R, int NX, int NY>
+SS_DEV void pack_lin(R (&r)[Rec<R, NX, NY>::LIN_P], const Lin<R, NX, NY>& l) {
+  typedef Rec<R, NX, NY> Q;
+  int o = 0;
+  pack<R, NX, NX>(r, o, l.F); o += NX * NX;
+  pack_tri<R, NX>(r, o, l.cQ); o += Q::TX;
+  pack_vec<R, NX>(r, o, l.bq); o += NX;
+  pack<R, NY, NX>(r, o, l.H); o += NY * NX;
+  pack_tri<R, NY>(r, o, l.cR); o += Q::TY;
+  pack_vec<R, NY>(r, o, l.c); o += NY;
+  SS_UNROLL
+  for (int k = Q::LIN; k < Q::LIN_P; ++k) r[k] = R(0);
+}
+
+template <typename R, int NX, int NY>
+SS_DEV void unpack_lin(const R (&r)[Rec<R, NX, NY>::LIN_P], Lin<R, NX, NY>& l) {
+  typedef Rec<R, NX, NY> Q;
+  int o = 0;
+  unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
+  unpack_tri<R, NX>(r, o, l.cQ); o += Q::TX;
+  unpack_vec<R, NX>(r, o, l.bq); o += NX;
+  unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
+  unpack_tri<R, NY>(r, o, l.cR); o += Q::TY;
+  unpack_vec<R, NY>(r, o, l.c);
+}
+
+template <typename R, int NX, int NY>
 SS_DEV void load_lin(const R* p, Lin<R, NX, NY>& l) {
   typedef Rec<R, NX, NY> Q;
   R r[Q::LIN_P];
   load_rec<R, Q::LIN>(p, r);
-  int o = 0;
-  unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  unpack_lower<R, NX>(r, o, l.cQ); o += NX * NX;
-  unpack_vec<R, NX>(r, o, l.bq); o += NX;
-  unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  unpack_lower<R, NY>(r, o, l.cR); o += NY * NY;
-  unpack_vec<R, NY>(r, o, l.c);
+  unpack_lin<R, NX, NY>(r, l);
 }
 
 template <typename R, int NX, int NY>
 SS_DEV void store_lin(R* p, const Lin<R, NX, NY>& l) {
   typedef Rec<R, NX, NY> Q;
   R r[Q::LIN_P];
-  int o = 0;
-  pack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  pack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
-  pack_vec<R, NX>(r, o, l.bq); o += NX;
-  pack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  pack<R, NY, NY>(r, o, l.cR); o += NY * NY;
-  pack_vec<R, NY>(r, o, l.c); o += NY;
-  SS_UNROLL
-  for (int k = Q::LIN; k < Q::LIN_P; ++k) r[k] = R(0);
+  pack_lin<R, NX, NY>(r, l);
   store_rec<R, Q::LIN>(p, r);
 }
 
@@ -80,7 +95,7 @@ SS_DEV void load_fe(const R* p, FElem<R, NX>& e) {
   int o = 0;
   unpack<R, NX, NX>(r, o, e.A); o += NX * NX;
   unpack_vec<R, NX>(r, o, e.b); o += NX;
-  unpack_lower<R, NX>(r, o, e.U); o += NX * NX;
+  unpack_tri<R, NX>(r, o, e.U); o += Q::TX;
   unpack_vec<R, NX>(r, o, e.eta); o += NX;
   unpack<R, NX, NX>(r, o, e.Z);
 }
@@ -92,7 +107,7 @@ SS_DEV void store_fe(R* p, const FElem<R, NX>& e) {
   int o = 0;
   pack<R, NX, NX>(r, o, e.A); o += NX * NX;
   pack_vec<R, NX>(r, o, e.b); o += NX;
-  pack<R, NX, NX>(r, o, e.U); o += NX * NX;
+  pack_tri<R, NX>(r, o, e.U); o += Q::TX;
   pack_vec<R, NX>(r, o, e.eta); o += NX;
   pack<R, NX, NX>(r, o, e.Z); o += NX * NX;
   SS_UNROLL
@@ -101,26 +116,37 @@ SS_DEV void store_fe(R* p, const FElem<R, NX>& e) {
 }
 
 template <typename R, int NX>
+SS_DEV void pack_se(R (&r)[Rec<R, NX, 1>::SE_P], const SElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
+  int o = 0;
+  pack_vec<R, NX>(r, o, e.g); o += NX;
+  pack<R, NX, NX>(r, o, e.E); o += NX * NX;
+  pack_tri<R, NX>(r, o, e.D); o += Q::TX;
+  SS_UNROLL
+  for (int k = Q::SE; k < Q::SE_P; ++k) r[k] = R(0);
+}
+
+template <typename R, int NX>
+SS_DEV void unpack_se(const R (&r)[Rec<R, NX, 1>::SE_P], SElem<R, NX>& e) {
+  int o = 0;
+  unpack_vec<R, NX>(r, o, e.g); o += NX;
+  unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
+  unpack_tri<R, NX>(r, o, e.D);
+}
+
+template <typename R, int NX>
 SS_DEV void load_se(const R* p, SElem<R, NX>& e) {
   typedef Rec<R, NX, 1> Q;
   R r[Q::SE_P];
   load_rec<R, Q::SE>(p, r);
-  int o = 0;
-  unpack_vec<R, NX>(r, o, e.g); o += NX;
-  unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  unpack_lower<R, NX>(r, o, e.D);
+  unpack_se<R, NX>(r, e);
 }
 
 template <typename R, int NX>
 SS_DEV void store_se(R* p, const SElem<R, NX>& e) {
   typedef Rec<R, NX, 1> Q;
   R r[Q::SE_P];
-  int o = 0;
-  pack_vec<R, NX>(r, o, e.g); o += NX;
-  pack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  pack<R, NX, NX>(r, o, e.D); o += NX * NX;
-  SS_UNROLL
-  for (int k = Q::SE; k < Q::SE_P; ++k) r[k] = R(0);
+  pack_se<R, NX>(r, e);
   store_rec<R, Q::SE>(p, r);
 }
 
@@ -130,7 +156,7 @@ SS_DEV void load_st(const R* p, State<R, NX>& s) {
   R r[Q::ST_P];
   load_rec<R, Q::ST>(p, r);
   unpack_vec<R, NX>(r, 0, s.m);
-  unpack_lower<R, NX>(r, NX, s.L);
+  unpack_tri<R, NX>(r, NX, s.L);
 }
 
 template <typename R, int NX>
@@ -138,7 +164,7 @@ SS_DEV void store_st(R* p, const State<R, NX>& s) {
   typedef Rec<R, NX, 1> Q;
   R r[Q::ST_P];
   pack_vec<R, NX>(r, 0, s.m);
-  pack<R, NX, NX>(r, NX, s.L);
+  pack_tri<R, NX>(r, NX, s.L);
   SS_UNROLL
   for (int k = Q::ST; k < Q::ST_P; ++k) r[k] = R(0);
   store_rec<R, Q::ST>(p, r);

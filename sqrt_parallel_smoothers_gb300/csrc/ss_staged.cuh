@@ -9,49 +9,7 @@
 
 namespace ss {
 
-template <typename R, int NX, int NY>
-SS_DEV void pack_lin(R (&r)[Rec<R, NX, NY>::LIN_P], const Lin<R, NX, NY>& l) {
-  typedef Rec<R, NX, NY> Q;
-  int o = 0;
-  pack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  pack<R, NX, NX>(r, o, l.cQ); o += NX * NX;
-  pack_vec<R, NX>(r, o, l.bq); o += NX;
-  pack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  pack<R, NY, NY>(r, o, l.cR); o += NY * NY;
-  pack_vec<R, NY>(r, o, l.c); o += NY;
-  SS_UNROLL
-  for (int k = Q::LIN; k < Q::LIN_P; ++k) r[k] = R(0);
-}
-
-template <typename R, int NX, int NY>
-SS_DEV void unpack_lin(const R (&r)[Rec<R, NX, NY>::LIN_P], Lin<R, NX, NY>& l) {
-  int o = 0;
-  unpack<R, NX, NX>(r, o, l.F); o += NX * NX;
-  unpack_lower<R, NX>(r, o, l.cQ); o += NX * NX;
-  unpack_vec<R, NX>(r, o, l.bq); o += NX;
-  unpack<R, NY, NX>(r, o, l.H); o += NY * NX;
-  unpack_lower<R, NY>(r, o, l.cR); o += NY * NY;
-  unpack_vec<R, NY>(r, o, l.c);
-}
-
-template <typename R, int NX>
-SS_DEV void pack_se(R (&r)[Rec<R, NX, 1>::SE_P], const SElem<R, NX>& e) {
-  typedef Rec<R, NX, 1> Q;
-  int o = 0;
-  pack_vec<R, NX>(r, o, e.g); o += NX;
-  pack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  pack<R, NX, NX>(r, o, e.D); o += NX * NX;
-  SS_UNROLL
-  for (int k = Q::SE; k < Q::SE_P; ++k) r[k] = R(0);
-}
-
-template <typename R, int NX>
-SS_DEV void unpack_se(const R (&r)[Rec<R, NX, 1>::SE_P], SElem<R, NX>& e) {
-  int o = 0;
-  unpack_vec<R, NX>(r, o, e.g); o += NX;
-  unpack<R, NX, NX>(r, o, e.E); o += NX * NX;
-  unpack_lower<R, NX>(r, o, e.D);
-}
+// Records are packed and unpacked by the functions of ss_pipeline.cuh.
 
 constexpr int STAGED_BLOCK = 128;
 // Minimum resident blocks per SM requested from the register allocator for the
@@ -67,7 +25,36 @@ constexpr int STAGED_BLOCK = 128;
 #ifndef SS_SCAN_MINB
 #define SS_SCAN_MINB 1
 #endif
+#ifndef SS_LEAF_MINB
+#define SS_LEAF_MINB SS_SCAN_MINB
+#endif
+#ifndef SS_WALK_ACC_SMEM
+#define SS_WALK_ACC_SMEM 1
+#endif
+#ifndef SS_WALK_Y_PREFETCH
+#define SS_WALK_Y_PREFETCH 1
+#endif
 constexpr int STAGED_WARPS = STAGED_BLOCK / 32;
+
+// A smoothing summary held in shared memory, one column per thread (element q
+// of thread t at col[q * STAGED_BLOCK + t]): conflict-free and off the
+// register file between the per-step folds.
+template <typename R, int NX>
+SS_DEV void col_load_se(const R* col, SElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
+  R r[Q::SE_P];
+  SS_UNROLL
+  for (int q = 0; q < Q::SE_P; ++q) r[q] = q < Q::SE ? col[q * STAGED_BLOCK] : R(0);
+  unpack_se<R, NX>(r, e);
+}
+template <typename R, int NX>
+SS_DEV void col_store_se(R* col, const SElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
+  R r[Q::SE_P];
+  pack_se<R, NX>(r, e);
+  SS_UNROLL
+  for (int q = 0; q < Q::SE; ++q) col[q * STAGED_BLOCK] = r[q];
+}
 
 // Dynamic shared memory (bytes) of each staged kernel.
 template <typename R, int NX, int NY>
@@ -75,7 +62,11 @@ struct StagedSmem {
   typedef Rec<R, NX, NY> Q;
   static constexpr size_t lin = sizeof(R) * STAGED_WARPS * StageTile<R, Q::LIN>::WARP_ELEMS;
   static constexpr size_t leaf = 2 * lin;
-  static constexpr size_t fwalk = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS;
+  // the filter walk keeps each thread's chunk smoothing summary in shared
+  // memory (FP32), one column per thread
+  static constexpr bool walk_acc_smem = SS_WALK_ACC_SMEM && sizeof(R) == 4;
+  static constexpr size_t walk_acc = walk_acc_smem ? sizeof(R) * STAGED_BLOCK * Q::SE : 0;
+  static constexpr size_t fwalk = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS + walk_acc;
   static constexpr size_t swalk = sizeof(R) * STAGED_WARPS *
                                   (2 * StageTile<R, Q::SE>::WARP_ELEMS + 32 * ((NX * NX) | 1));
 };
@@ -137,7 +128,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY>
-__global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_leaf_staged_kernel(ScanArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, SS_LEAF_MINB) filter_leaf_staged_kernel(ScanArgs<R> a) {
   typedef Rec<R, NX, NY> Q;
   typedef StageTile<R, Q::LIN> TL;
   extern __shared__ __align__(16) unsigned char ss_smem[];
@@ -190,6 +181,8 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
   extern __shared__ __align__(16) unsigned char ss_smem[];
   R* tiles = warp_smem<R>(ss_smem, 2 * TL::WARP_ELEMS);
   R* stile = reinterpret_cast<R*>(ss_smem) + STAGED_WARPS * 2 * TL::WARP_ELEMS + (threadIdx.x >> 5) * TS::WARP_ELEMS;
+  constexpr bool ACC_SMEM = StagedSmem<R, NX, NY>::walk_acc_smem;
+  R* acol = reinterpret_cast<R*>(ss_smem) + STAGED_WARPS * (2 * TL::WARP_ELEMS + TS::WARP_ELEMS) + threadIdx.x;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool work = j < a.g.lvl[1][a.g.B];
   int64_t i = 0, t0 = 0, t1 = 0;
@@ -206,11 +199,20 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
   cp_async_commit();
   SElem<R, NX> acc;
   double ll = 0.0;
+  R yn[NY];   // observation of the step (read one step ahead)
+  SS_UNROLL
+  for (int q = 0; q < NY; ++q) yn[q] = (SS_WALK_Y_PREFETCH && n > 0) ? a.ys[first * NY + q] : R(0);
   for (int k = 0; k < a.g.C; ++k) {
     if (!__any_sync(FULL_MASK, k < n)) break;
     stage_load_async<R, Q::LIN>(k + 1 < n ? a.lin + (first + k + 1) * Q::LIN_P : nullptr,
                                 tiles + ((k + 1) & 1) * TL::WARP_ELEMS);
     cp_async_commit();
+    R y[NY];
+    SS_UNROLL
+    for (int q = 0; q < NY; ++q) {
+      y[q] = yn[q];
+      if (SS_WALK_Y_PREFETCH && k + 1 < n) yn[q] = a.ys[(first + k + 1) * NY + q];
+    }
     cp_async_wait<1>();
     __syncwarp();
     // Order within a step, chosen by measurement: the smoothing element is
@@ -235,16 +237,28 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
         stage_store<R, Q::SE>(stile, srec, k < n ? a.selem + (first + k) * Q::SE_P : nullptr);
     }
     if (k < n && a.emit_smoother) {
-      if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
+      if constexpr (ACC_SMEM) {
+        if (k == 0) {
+          col_store_se<R, NX>(acol, se);
+        } else {
+          SElem<R, NX> ac;
+          col_load_se<R, NX>(acol, ac);
+          smoother_fold<R, NX>(ac, se);
+          col_store_se<R, NX>(acol, ac);
+        }
+      } else {
+        if (k == 0) acc = se; else smoother_fold<R, NX>(acc, se);
+      }
     }
     if (k < n) {
       R rec[Q::LIN_P];
       stage_read<R, Q::LIN>(tile, rec);
       Lin<R, NX, NY> l;
       unpack_lin<R, NX, NY>(rec, l);
-      R y[NY];
-      SS_UNROLL
-      for (int q = 0; q < NY; ++q) y[q] = a.ys[(first + k) * NY + q];
+      if (!SS_WALK_Y_PREFETCH) {
+        SS_UNROLL
+        for (int q = 0; q < NY; ++q) y[q] = a.ys[(first + k) * NY + q];
+      }
       ll += (double)filter_update<R, NX, NY>(s, l, y, X, mp);
       if (a.filt_m != nullptr) store_traj<R, NX>(a.filt_m, a.filt_L, first + i + k + 1, s);
     }
@@ -252,7 +266,10 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
   }
   cp_async_wait<0>();
   if (work) {
-    if (a.emit_smoother) store_se<R, NX>(a.ssum[1] + j * Q::SE_P, acc);
+    if (a.emit_smoother) {
+      if constexpr (ACC_SMEM) col_load_se<R, NX>(acol, acc);
+      store_se<R, NX>(a.ssum[1] + j * Q::SE_P, acc);
+    }
     if (a.ll_chunk != nullptr) a.ll_chunk[j] = ll;
     if (t1 == a.g.off[i + 1] - base) store_st<R, NX>(a.fT + i * Q::ST_P, s);
   }
