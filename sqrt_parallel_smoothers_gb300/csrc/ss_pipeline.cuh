@@ -71,6 +71,43 @@ SS_DEV void unpack_lin(const R (&r)[Rec<R, NX, NY>::LIN_P], Lin<R, NX, NY>& l) {
   unpack_vec<R, NY>(r, o, l.c);
 }
 
+// The two halves of pack_lin written straight into a record row (shared
+// memory), in the same layout.
+template <typename R, int NX, int NY>
+SS_DEV void write_lin_transition(R* row, const R (&F)[NX][NX], const R (&cQ)[NX][NX], const R (&bq)[NX]) {
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) row[i * NX + j] = F[i][j];
+  }
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) {
+    SS_UNROLL
+    for (int j = 0; j <= i; ++j) row[NX * NX + i * (i + 1) / 2 + j] = cQ[i][j];
+  }
+  SS_UNROLL
+  for (int i = 0; i < NX; ++i) row[NX * NX + Rec<R, NX, NY>::TX + i] = bq[i];
+}
+template <typename R, int NX, int NY>
+SS_DEV void write_lin_observation(R* row, const R (&H)[NY][NX], const R (&cR)[NY][NY], const R (&c)[NY]) {
+  typedef Rec<R, NX, NY> Q;
+  constexpr int o = NX * NX + Q::TX + NX;
+  SS_UNROLL
+  for (int i = 0; i < NY; ++i) {
+    SS_UNROLL
+    for (int j = 0; j < NX; ++j) row[o + i * NX + j] = H[i][j];
+  }
+  SS_UNROLL
+  for (int i = 0; i < NY; ++i) {
+    SS_UNROLL
+    for (int j = 0; j <= i; ++j) row[o + NY * NX + i * (i + 1) / 2 + j] = cR[i][j];
+  }
+  SS_UNROLL
+  for (int i = 0; i < NY; ++i) row[o + NY * NX + Q::TY + i] = c[i];
+  SS_UNROLL
+  for (int q = Q::LIN; q < Q::LIN_P; ++q) row[q] = R(0);
+}
+
 template <typename R, int NX, int NY>
 SS_DEV void load_lin(const R* p, Lin<R, NX, NY>& l) {
   typedef Rec<R, NX, NY> Q;

@@ -85,6 +85,31 @@ SS_DEV void stage_store(R* tile, const R (&src)[Padded<R, N>::n], R* dst) {
   __syncwarp();
 }
 
+// Two-phase form of stage_store for records built in parts: each lane writes
+// its row (stage_row) element by element, then the warp copies every lane's
+// row to its destination (stage_flush).
+template <typename R, int N>
+SS_DEV R* stage_row(R* tile) {
+  return tile + (threadIdx.x & 31) * StageTile<R, N>::STRIDE;
+}
+template <typename R, int N>
+SS_DEV void stage_flush(const R* tile, R* dst) {
+  typedef StageTile<R, N> S;
+  typedef typename Vec16<R>::type V;
+  const int lane = threadIdx.x & 31;
+  __syncwarp();
+  const unsigned long long mine = reinterpret_cast<unsigned long long>(dst);
+  SS_UNROLL
+  for (int it = 0; it < S::NV; ++it) {
+    const int q = it * 32 + lane;
+    const int r = q / S::NV;
+    const int p = q - r * S::NV;
+    R* g = reinterpret_cast<R*>(__shfl_sync(FULL_MASK, mine, r));
+    if (g != nullptr) reinterpret_cast<V*>(g)[p] = reinterpret_cast<const V*>(tile + r * S::STRIDE)[p];
+  }
+  __syncwarp();
+}
+
 // Element-granular variant for destinations without 16-byte alignment (the
 // caller's trajectory rows): W elements per lane, row stride W | 1.
 template <typename R, int W>

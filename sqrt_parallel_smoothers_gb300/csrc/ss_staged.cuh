@@ -89,29 +89,31 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
     i = find_seq(a.off, a.B, k);
     if (a.active != nullptr && a.active[i] == 0) work = false;
   }
-  R rec[Q::LIN_P];
-  SS_UNROLL
-  for (int q = 0; q < Q::LIN_P; ++q) rec[q] = R(0);  // idle lanes stage zeros (never stored)
+  // The record is written into this lane's shared row in two parts, the
+  // transition's before the observation is linearised, so the transition's
+  // results do not stay live in registers.
+  R* row = stage_row<R, Q::LIN>(tile);
   if (work) {
     const int64_t t = k - a.off[i];
     const int64_t s = a.off[i] + i + t;
-    Lin<R, NX, NY> l;
     {
       TF f;
       f.init(a.tm);
-      R m[NX], C[NX][NX], qm[NX], qL[NX][NX];
+      R m[NX], C[NX][NX], qm[NX], qL[NX][NX], F[NX][NX], cQ[NX][NX], bq[NX];
       load_nominal<R, NX>(a.nom_m, a.nom_L, s, m, C);
       load_noise<R, NX>(a.tq_m, a.tq_L, qm, qL);
-      linearize<R, NX, NX, TF, METHOD>(f, m, C, qm, qL, a.rule, a.slr_form, l.F, l.cQ, l.bq);
+      linearize<R, NX, NX, TF, METHOD>(f, m, C, qm, qL, a.rule, a.slr_form, F, cQ, bq);
+      write_lin_transition<R, NX, NY>(row, F, cQ, bq);
     }
+    R H[NY][NX], cR[NY][NY], c[NY];
     if (a.trans_only) {
       SS_UNROLL
       for (int r = 0; r < NY; ++r) {
-        l.c[r] = R(0);
+        c[r] = R(0);
         SS_UNROLL
-        for (int jj = 0; jj < NX; ++jj) l.H[r][jj] = R(0);
+        for (int jj = 0; jj < NX; ++jj) H[r][jj] = R(0);
         SS_UNROLL
-        for (int jj = 0; jj < NY; ++jj) l.cR[r][jj] = R(0);
+        for (int jj = 0; jj < NY; ++jj) cR[r][jj] = R(0);
       }
     } else {
       OF h;
@@ -119,11 +121,11 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
       R m[NX], C[NX][NX], qm[NY], qL[NY][NY];
       load_nominal<R, NX>(a.nom_m, a.nom_L, s + 1, m, C);
       load_noise<R, NY>(a.oq_m, a.oq_L, qm, qL);
-      linearize<R, NX, NY, OF, METHOD>(h, m, C, qm, qL, a.rule, a.slr_form, l.H, l.cR, l.c);
+      linearize<R, NX, NY, OF, METHOD>(h, m, C, qm, qL, a.rule, a.slr_form, H, cR, c);
     }
-    pack_lin<R, NX, NY>(rec, l);
+    write_lin_observation<R, NX, NY>(row, H, cR, c);
   }
-  stage_store<R, Q::LIN>(tile, rec, work ? a.out + k * Q::LIN_P : nullptr);
+  stage_flush<R, Q::LIN>(tile, work ? a.out + k * Q::LIN_P : nullptr);
 }
 
 // ---------------------------------------------------------------------------
