@@ -240,8 +240,8 @@ ALG_BYTES_PER_STEP = {
     "smoother_walk": 4 * (45 + 20),  # smoothing element in, smoothed state out
 }
 # DRAM bytes (read + write) per timestep of each kernel, from one ncu capture of this workload
-# (profiles/staged_kernels_bearings_b1024_c32g4.md: bytes of one launch / 1,101,870 timesteps)
-TRAFFIC_BYTES_PER_STEP = {"lin": 357, "filter_leaf": 306, "filter_walk": 503, "smoother_walk": 340}
+# (profiles/staged_kernels_bearings_b1024_c16g4.md: bytes of one launch / 1,101,870 timesteps)
+TRAFFIC_BYTES_PER_STEP = {"lin": 308, "filter_leaf": 269, "filter_walk": 428, "smoother_walk": 324}
 
 
 def adjoint_section(torch, S, flush):
