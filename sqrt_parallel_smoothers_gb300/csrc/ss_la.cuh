@@ -21,12 +21,43 @@ SS_DEV double ss_log(double x) { return log(x); }
 SS_DEV bool ss_isfinite(float x) { return isfinite(x); }
 SS_DEV bool ss_isfinite(double x) { return isfinite(x); }
 
-// Correctly rounded reciprocal (the triangular solves' pivots); other scalar
-// types (dual numbers) use their division.
-SS_DEV float ss_rcp(float x) { return __frcp_rn(x); }
+// FP32 factorisations use the hardware reciprocal and reciprocal square root
+// (__fdividef, rsqrtf: within 2 ulp) in the Householder reflectors and the
+// triangular solves' pivots; FP64 stays correctly rounded.  Other scalar types
+// (dual numbers) use their division.
+#ifndef SS_FAST_FP32
+#define SS_FAST_FP32 1
+#endif
+SS_DEV float ss_rcp(float x) { return SS_FAST_FP32 ? __fdividef(1.0f, x) : __frcp_rn(x); }
 SS_DEV double ss_rcp(double x) { return __drcp_rn(x); }
 template <typename R>
 SS_DEV R ss_rcp(const R& x) { return R(1) / x; }
+
+// One Householder reflector's scalars from x0 = M[i][i] and sigma = the sum of
+// squares of the rest of row i (> 0): beta = -sign(x0) sqrt(x0^2 + sigma),
+// v0 = x0 - beta and k = 1 / (beta v0) = -1 / (|beta| (|beta| + |x0|)).
+template <typename R>
+SS_DEV void reflector(R x0, R sigma, R& beta, R& v0, R& k) {
+  const R nrm = ss_sqrt(x0 * x0 + sigma);
+  beta = (x0 <= R(0)) ? nrm : -nrm;   // opposite sign of x0: no cancellation in v0
+  v0 = x0 - beta;
+  k = R(1) / (beta * v0);
+}
+SS_DEV void reflector(float x0, float sigma, float& beta, float& v0, float& k) {
+  if (SS_FAST_FP32) {
+    const float s = x0 * x0 + sigma;
+    const float ri = rsqrtf(s);
+    const float nrm = s * ri;
+    beta = (x0 <= 0.0f) ? nrm : -nrm;
+    v0 = x0 - beta;
+    k = __fdividef(-ri, nrm + fabsf(x0));
+  } else {
+    const float nrm = sqrtf(x0 * x0 + sigma);
+    beta = (x0 <= 0.0f) ? nrm : -nrm;
+    v0 = x0 - beta;
+    k = 1.0f / (beta * v0);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // tria: on return M[:, :ROWS] holds the lower-triangular L (diag >= 0) with
@@ -172,10 +203,8 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
       if (sigma != R(0)) {
         // H = I + u u^T / (beta v0), u = (v0, M[i][i+1:]), v0 = x0 - beta:
         // one reciprocal per reflector, no scaled copy of the row.
-        const R nrm = ss_sqrt(x0 * x0 + sigma);
-        beta = (x0 <= R(0)) ? nrm : -nrm;   // opposite sign of x0: no cancellation in v0
-        const R v0 = x0 - beta;
-        const R k = R(1) / (beta * v0);
+        R v0, k;
+        reflector(x0, sigma, beta, v0, k);
         SS_UNROLL
         for (int r = i + 1; r < ROWS; ++r) {
           if ((TOUCH >> r) & 1) {
