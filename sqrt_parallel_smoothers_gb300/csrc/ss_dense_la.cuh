@@ -116,6 +116,31 @@ SS_DEV void store_part(R* M, int r, const R (&x)[CPX]) {
 
 // ----------------------------------------------------------------------------- tria
 
+// Parlett's reflector for x = (x0, rest), sig = |rest|^2: v0 = x0 - |x| computed
+// without cancellation, tau = 2 / (v0^2 + sig) (0 for a zero vector).  FP32 uses
+// the hardware reciprocal square root and reciprocal (within 2 ulp).
+template <typename R>
+SS_DEV void parlett(R x0, R sig, R& v0, R& tau) {
+  const R nrm = ss_sqrt(x0 * x0 + sig);
+  v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
+  const R vv = v0 * v0 + sig;
+  tau = (vv > R(0)) ? R(2) / vv : R(0);
+}
+SS_DEV void parlett(float x0, float sig, float& v0, float& tau) {
+  if (!SS_FAST_FP32) {
+    const float nrm = sqrtf(x0 * x0 + sig);
+    v0 = (x0 <= 0.0f) ? x0 - nrm : -sig / (x0 + nrm);
+    const float vv = v0 * v0 + sig;
+    tau = (vv > 0.0f) ? 2.0f / vv : 0.0f;
+    return;
+  }
+  const float s = x0 * x0 + sig;
+  const float nrm = (s > 0.0f) ? s * rsqrtf(s) : 0.0f;
+  v0 = (x0 <= 0.0f) ? x0 - nrm : __fdividef(-sig, x0 + nrm);
+  const float vv = v0 * v0 + sig;
+  tau = (vv > 0.0f) ? __fdividef(2.0f, vv) : 0.0f;
+}
+
 // M <- [L 0] = M Q, Q orthogonal, L lower triangular with a non-negative
 // diagonal: Householder reflections from the right (Golub & Van Loan,
 // Algorithm 5.1.1, with Parlett's formula for the sign-free reflector, so the
@@ -170,10 +195,8 @@ struct Tria {
       __syncwarp();
       const R sig = v[CP];
       const R x0 = v[p];
-      const R nrm = ss_sqrt(x0 * x0 + sig);
-      const R v0 = (x0 <= R(0)) ? x0 - nrm : -sig / (x0 + nrm);
-      const R vv = v0 * v0 + sig;
-      const R tau = (vv > R(0)) ? R(2) / vv : R(0);
+      R v0, tau;
+      parlett(x0, sig, v0, tau);
       // v - x on the pivot block: -x_j left of p, v_p - x_p at p, 0 right of p
       R cb[JB - J0];
       SS_UNROLL
@@ -365,7 +388,7 @@ SS_DEV void trsm_rl(R* X, const R* L) {
     load_row<R, N, LDX>(X, ii, x);
     SS_UNROLL
     for (int k = N - 1; k >= 0; --k) {
-      x[k] = x[k] / L[k * LDL + k];
+      x[k] = x[k] * ss_rcp(L[k * LDL + k]);
       SS_UNROLL
       for (int j = 0; j < k; j += W) {
         const Vec<R> l = ld16(L + k * LDL + j);
@@ -401,7 +424,7 @@ SS_DEV void trsm_rlt(R* X, const R* L) {
         for (int u = 0; u < W; ++u)
           if (j + u < k) t -= x[j + u] * l.v[u];
       }
-      x[k] = t / L[k * LDL + k];
+      x[k] = t * ss_rcp(L[k * LDL + k]);
     }
     __syncwarp();
     if (i < ROWS) store_row<R, N, LDX>(X, i, x);

@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
         if (r >= NX && r < 2 * NX) {
           SS_UNROLL
           for (int k = NX - 1; k >= 0; --k) {
-            row[s][k] = row[s][k] / L[k * S::LDN + k];
+            row[s][k] = row[s][k] * ss_rcp(L[k * S::LDN + k]);
             SS_UNROLL
             for (int jj = 0; jj < k; jj += W) {
               const Vec<R> lv = ld16(L + k * S::LDN + jj);

@@ -286,6 +286,7 @@ struct LinArgs {
   int64_t B, total;
   const R* nom_m;        // nominal trajectory or null (zero means, identity factors)
   const R* nom_L;
+  const R* nom_rec;      // or the nominal as packed state records (m, lower L)
   const int32_t* active; // null or B flags
   ModelArgs<R> tm, om;
   const R* tq_m;         // transition noise mean / chol
@@ -297,6 +298,7 @@ struct LinArgs {
   int trans_only;
   R* out;                // per-step Lin records
 };
+
 
 template <typename R, int N>
 SS_DEV void load_nominal(const R* nm, const R* nL, int64_t s, R (&m)[N], R (&C)[N][N]) {
@@ -316,6 +318,25 @@ SS_DEV void load_nominal(const R* nm, const R* nL, int64_t s, R (&m)[N], R (&C)[
     }
   }
 }
+
+// The nominal state at s from LinArgs: packed records, the caller's layout, or
+// the default (zero mean, identity factor).
+template <typename R, int NX>
+SS_DEV void load_nominal_any(const LinArgs<R>& a, int64_t s, R (&m)[NX], R (&C)[NX][NX]) {
+  if (a.nom_rec != nullptr) {
+    State<R, NX> st;
+    load_st<R, NX>(a.nom_rec + s * Rec<R, NX, 1>::ST_P, st);
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      m[r] = st.m[r];
+      SS_UNROLL
+      for (int c = 0; c < NX; ++c) C[r][c] = st.L[r][c];
+    }
+  } else {
+    load_nominal<R, NX>(a.nom_m, a.nom_L, s, m, C);
+  }
+}
+
 
 template <typename R, int D>
 SS_DEV void load_noise(const R* qm, const R* qL, R (&m)[D], R (&L)[D][D]) {
@@ -426,8 +447,10 @@ struct ScanArgs {
   const R* in_L;
   R* out_m;                // smoothed trajectory
   R* out_L;
+  R* out_rec;              // or the smoothed trajectory as packed state records
   const R* prev_m;         // nominal means of this pass (convergence test) or null
   const R* prev_L;
+  const R* prev_rec;       // or the nominal as packed state records
   double* mse;             // (B) accumulated squared mean change or null
   uint32_t* flags;         // (B) status bits or null
 };
@@ -649,7 +672,8 @@ SS_DEV void accumulate_change(const ScanArgs<R>& a, int64_t i, int64_t s, const 
     double d2 = 0.0;
     SS_UNROLL
     for (int r = 0; r < NX; ++r) {
-      const double d = (double)st.m[r] - (double)a.prev_m[s * NX + r];
+      const R pm = a.prev_rec != nullptr ? a.prev_rec[s * Rec<R, NX, 1>::ST_P + r] : a.prev_m[s * NX + r];
+      const double d = (double)st.m[r] - (double)pm;
       d2 += d * d;
     }
     atomicAdd(a.mse + i, d2);
@@ -662,11 +686,19 @@ SS_DEV void accumulate_change(const ScanArgs<R>& a, int64_t i, int64_t s, const 
   }
 }
 
+// The smoothed state at s into the output trajectory (caller's layout or packed records).
+template <typename R, int NX>
+SS_DEV void store_out(const ScanArgs<R>& a, int64_t s, const State<R, NX>& st) {
+  if (a.out_rec != nullptr) store_st<R, NX>(a.out_rec + s * Rec<R, NX, 1>::ST_P, st);
+  else store_traj<R, NX>(a.out_m, a.out_L, s, st);
+}
+
 template <typename R, int NX>
 SS_DEV void copy_state(const ScanArgs<R>& a, int64_t s) {
   State<R, NX> st;
-  load_traj<R, NX>(a.prev_m, a.prev_L, s, st);
-  store_traj<R, NX>(a.out_m, a.out_L, s, st);
+  if (a.prev_rec != nullptr) load_st<R, NX>(a.prev_rec + s * Rec<R, NX, 1>::ST_P, st);
+  else load_traj<R, NX>(a.prev_m, a.prev_L, s, st);
+  store_out<R, NX>(a, s, st);
 }
 
 template <typename R, int NX>
@@ -682,7 +714,7 @@ __global__ void __launch_bounds__(128) smoother_top_kernel(ScanArgs<R> a) {
   }
   State<R, NX> s;
   load_st<R, NX>(a.fT + i * Q::ST_P, s);
-  store_traj<R, NX>(a.out_m, a.out_L, sT, s);
+  store_out<R, NX>(a, sT, s);
   accumulate_change<R, NX>(a, i, sT, s);
   const int L = a.g.L;
   const int64_t b = a.g.lvl[L][i], e = a.g.lvl[L][i + 1];
@@ -735,7 +767,7 @@ __global__ void __launch_bounds__(128) smoother_walk_kernel(ScanArgs<R> a) {
     SElem<R, NX> e;
     load_se<R, NX>(a.selem + (base + t) * Q::SE_P, e);
     smoother_apply<R, NX>(s, e);
-    store_traj<R, NX>(a.out_m, a.out_L, base + i + t, s);
+    store_out<R, NX>(a, base + i + t, s);
     accumulate_change<R, NX>(a, i, base + i + t, s);
   }
 }

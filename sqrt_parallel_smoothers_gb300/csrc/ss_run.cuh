@@ -346,9 +346,10 @@ struct Runner {
     return SS_OK;
   }
 
-  int lin(const R* nm, const R* nL, const int32_t* active, bool trans_only) {
+  int lin(const R* nm, const R* nL, const int32_t* active, bool trans_only, const R* nrec = nullptr) {
     la.nom_m = nm;
     la.nom_L = nL;
+    la.nom_rec = nrec;
     la.active = active;
     la.trans_only = trans_only ? 1 : 0;
     return launch_lin<R, NX, NY>(la, p.transition.kind, trans_only ? SS_MODEL_LINEAR : p.observation.kind,
@@ -468,18 +469,25 @@ struct Runner {
     const int calls = c.n_iter > 1 ? c.n_iter : 1;
     R* bufm[2] = {at<R>(y.nomA_m), at<R>(y.nomB_m)};
     R* bufL[2] = {at<R>(y.nomA_L), at<R>(y.nomB_L)};
+    // Intermediate nominals are packed state records (m, lower L: whole 16-byte
+    // pieces, 80 bytes for nx = 5) in the factor buffers; only the caller's
+    // initial nominal and the final output use the caller's layout.  The
+    // dual-number kernels keep the caller's layout throughout.
+    constexpr bool packed = Vec16<R>::vec;
     const R* cur_m = static_cast<const R*>(c.nom_m);
     const R* cur_L = static_cast<const R*>(c.nom_L);
+    const R* cur_rec = nullptr;
     int next = 0;
     // pass 0 (init_nominal None): filter-smoother at the default nominal
     const int first = has_init ? 1 : 0;
     for (int k = first; k <= calls; ++k) {
       const bool last = (k == calls);
       const bool counted = (k >= 1);
-      R* om = last ? static_cast<R*>(c.out_m) : bufm[next];
-      R* oL = last ? static_cast<R*>(c.out_L) : bufL[next];
+      R* om = last ? static_cast<R*>(c.out_m) : (packed ? nullptr : bufm[next]);
+      R* oL = last ? static_cast<R*>(c.out_L) : (packed ? nullptr : bufL[next]);
+      R* orec = (!last && packed) ? bufL[next] : nullptr;
       const int32_t* act = (tol_mode && counted) ? active : nullptr;
-      rc = lin(cur_m, cur_L, act, false);
+      rc = lin(cur_m, cur_L, act, false, cur_rec);
       if (rc) return rc;
       sa.active = act;
       sa.filt_m = nullptr;
@@ -489,8 +497,10 @@ struct Runner {
       if (rc) return rc;
       sa.out_m = om;
       sa.out_L = oL;
+      sa.out_rec = orec;
       sa.prev_m = cur_m;
       sa.prev_L = cur_L;
+      sa.prev_rec = cur_rec;
       sa.mse = (tol_mode && counted) ? mse : nullptr;
       sa.flags = last ? c.out_flags : nullptr;
       rc = smoother_scan_and_walk();
@@ -500,8 +510,11 @@ struct Runner {
       }
       cur_m = om;
       cur_L = oL;
+      cur_rec = orec;
       next ^= 1;
     }
+    sa.out_rec = nullptr;
+    sa.prev_rec = nullptr;
     sa.active = nullptr;
     sa.mse = nullptr;
     sa.flags = nullptr;

@@ -67,8 +67,12 @@ struct StagedSmem {
   static constexpr bool walk_acc_smem = SS_WALK_ACC_SMEM && sizeof(R) == 4;
   static constexpr size_t walk_acc = walk_acc_smem ? sizeof(R) * STAGED_BLOCK * Q::SE : 0;
   static constexpr size_t fwalk = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS + walk_acc;
+  // the smoother walk's output tile: a row holds nx x nx words (the caller's
+  // layout) or one packed state record
+  static constexpr int out_stride = ((NX * NX) | 1) > StageTile<R, Q::ST>::STRIDE ? ((NX * NX) | 1)
+                                                                                  : StageTile<R, Q::ST>::STRIDE;
   static constexpr size_t swalk = sizeof(R) * STAGED_WARPS *
-                                  (2 * StageTile<R, Q::SE>::WARP_ELEMS + 32 * ((NX * NX) | 1));
+                                  (2 * StageTile<R, Q::SE>::WARP_ELEMS + 32 * out_stride);
 };
 
 template <typename R>
@@ -100,7 +104,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
       TF f;
       f.init(a.tm);
       R m[NX], C[NX][NX], qm[NX], qL[NX][NX], F[NX][NX], cQ[NX][NX], bq[NX];
-      load_nominal<R, NX>(a.nom_m, a.nom_L, s, m, C);
+      load_nominal_any<R, NX>(a, s, m, C);
       load_noise<R, NX>(a.tq_m, a.tq_L, qm, qL);
       linearize<R, NX, NX, TF, METHOD>(f, m, C, qm, qL, a.rule, a.slr_form, F, cQ, bq);
       write_lin_transition<R, NX, NY>(row, F, cQ, bq);
@@ -119,7 +123,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
       OF h;
       h.init(a.om);
       R m[NX], C[NX][NX], qm[NY], qL[NY][NY];
-      load_nominal<R, NX>(a.nom_m, a.nom_L, s + 1, m, C);
+      load_nominal_any<R, NX>(a, s + 1, m, C);
       load_noise<R, NY>(a.oq_m, a.oq_L, qm, qL);
       linearize<R, NX, NY, OF, METHOD>(h, m, C, qm, qL, a.rule, a.slr_form, H, cR, c);
     }
@@ -282,7 +286,7 @@ template <typename R, int NX>
 __global__ void __launch_bounds__(STAGED_BLOCK, SS_SWALK_MINB) smoother_walk_staged_kernel(ScanArgs<R> a) {
   typedef Rec<R, NX, 1> Q;
   typedef StageTile<R, Q::SE> TS;
-  constexpr int LW = (NX * NX) | 1;
+  constexpr int LW = StagedSmem<R, NX, 1>::out_stride;
   extern __shared__ __align__(16) unsigned char ss_smem[];
   R* tiles = warp_smem<R>(ss_smem, 2 * TS::WARP_ELEMS);
   R* otile = reinterpret_cast<R*>(ss_smem) + STAGED_WARPS * 2 * TS::WARP_ELEMS + (threadIdx.x >> 5) * 32 * LW;
@@ -328,8 +332,22 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SWALK_MINB) smoother_walk_sta
         for (int c = 0; c < NX; ++c) Lrow[r * NX + c] = (c <= r) ? s.L[r][c] : R(0);
       }
     }
-    stage_store_words<R, NX>(otile, mrow, k < n ? a.out_m + st * NX : nullptr);
-    stage_store_words<R, NX * NX>(otile, Lrow, k < n ? a.out_L + st * NX * NX : nullptr);
+    if (a.out_rec != nullptr) {
+      // packed state records (the next nominal): whole 16-byte pieces
+      R srec[Q::ST_P];
+      SS_UNROLL
+      for (int q = 0; q < Q::ST_P; ++q) srec[q] = R(0);
+      SS_UNROLL
+      for (int r = 0; r < NX; ++r) {
+        srec[r] = mrow[r];
+        SS_UNROLL
+        for (int c = 0; c <= r; ++c) srec[NX + r * (r + 1) / 2 + c] = Lrow[r * NX + c];
+      }
+      stage_store<R, Q::ST>(otile, srec, k < n ? a.out_rec + st * Q::ST_P : nullptr);
+    } else {
+      stage_store_words<R, NX>(otile, mrow, k < n ? a.out_m + st * NX : nullptr);
+      stage_store_words<R, NX * NX>(otile, Lrow, k < n ? a.out_L + st * NX * NX : nullptr);
+    }
   }
   cp_async_wait<0>();
 }
