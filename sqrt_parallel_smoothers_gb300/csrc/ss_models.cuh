@@ -21,8 +21,20 @@ template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_sin(const Dual<T, NT>& a) { return chain(a, ss_sin(a.v), ss_cos(a.v)); }
 template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_cos(const Dual<T, NT>& a) { return chain(a, ss_cos(a.v), -ss_sin(a.v)); }
-// sin and cos of one angle with one range reduction.
-SS_DEV void ss_sincos(float x, float& s, float& c) { sincosf(x, &s, &c); }
+// sin and cos of one angle with one range reduction.  In FP32 a small angle
+// (|x| <= 1/4, the coordinated turn's omega dt in practice) takes the Taylor
+// polynomials to degree 9 / 8, whose truncation error (below 3e-13) is far
+// under FP32 rounding; larger angles call sincosf.
+SS_DEV void ss_sincos(float x, float& s, float& c) {
+  if (fabsf(x) <= 0.25f) {
+    const float x2 = x * x;
+    s = x * (1.0f - x2 * (1.0f / 6.0f) * (1.0f - x2 * (1.0f / 20.0f) * (1.0f - x2 * (1.0f / 42.0f) *
+                                                                          (1.0f - x2 * (1.0f / 72.0f)))));
+    c = 1.0f - x2 * 0.5f * (1.0f - x2 * (1.0f / 12.0f) * (1.0f - x2 * (1.0f / 30.0f) * (1.0f - x2 * (1.0f / 56.0f))));
+  } else {
+    sincosf(x, &s, &c);
+  }
+}
 SS_DEV void ss_sincos(double x, double& s, double& c) { sincos(x, &s, &c); }
 template <typename T, int NT>
 SS_DEV void ss_sincos(const Dual<T, NT>& a, Dual<T, NT>& s, Dual<T, NT>& c) {
@@ -151,8 +163,9 @@ struct BearingsFn {
       const R r2 = dx * dx + dy * dy;
       SS_UNROLL
       for (int j = 0; j < DIN; ++j) J[k][j] = R(0);
-      J[k][0] = -dy / r2;
-      J[k][1] = dx / r2;
+      const R ir2 = ss_rcp(r2);
+      J[k][0] = -dy * ir2;
+      J[k][1] = dx * ir2;
     }
   }
 };
