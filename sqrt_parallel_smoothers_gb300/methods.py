@@ -813,6 +813,11 @@ class IteratedSmootherPlan:
                  init_nominal_trajectory=None, criterion=_default_criterion, return_loglikelihood=False, *,
                  lengths=None, offsets=None, chunk=0, group=0, slr_form=0, graph=True, profile=False,
                  streams=1):
+        self._ctor = ((observations, x0, transition_model, observation_model, linearization_method,
+                       init_nominal_trajectory, criterion, return_loglikelihood),
+                      dict(lengths=lengths, offsets=offsets, chunk=chunk, group=group, slr_form=slr_form,
+                           graph=graph, profile=False, streams=streams))
+        self._twin_plan, self._copy_stream, self._flip = None, None, 0
         method = _check_common(x0, True, linearization_method)
         if init_nominal_trajectory is not None:
             are_inputs_compatible(x0, init_nominal_trajectory)
@@ -954,14 +959,48 @@ class IteratedSmootherPlan:
         """Copy new packed observations ``(sum T_i, ny)`` into the staged buffer."""
         self._args[0].copy_(ys_packed, non_blocking=non_blocking)
 
-    def run_host(self, ys_host, out_mean_host, out_chol_host=None):
-        """Host -> device copy of ``ys_host``, replay, device -> host copy of the results."""
-        self.set_observations(ys_host)
-        self.run()
-        out_mean_host.copy_(self.mean, non_blocking=True)
-        if out_chol_host is not None:
-            out_chol_host.copy_(self.chol, non_blocking=True)
+    def run_host(self, ys_host, out_mean_host, out_chol_host=None, pipelined=False):
+        """Host -> device copy of ``ys_host``, replay, device -> host copy of the results.
+
+        With ``pipelined=True`` calls alternate between this plan and a twin
+        (its own outputs and workspace, built at the first such call) and the
+        copy-out runs on a separate stream, so one call's device-to-host copy
+        overlaps the next call's smoother.  The host buffers are complete once
+        :meth:`sync_host` has been called (or the copy stream synchronised)."""
+        if not pipelined:
+            self.set_observations(ys_host)
+            self.run()
+            out_mean_host.copy_(self.mean, non_blocking=True)
+            if out_chol_host is not None:
+                out_chol_host.copy_(self.chol, non_blocking=True)
+            return out_mean_host, out_chol_host
+        dev = self._args[0].device
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream(dev)
+            self._events = [(torch.cuda.Event(), torch.cuda.Event()) for _ in range(2)]
+        if self._flip == 1 and self._twin_plan is None:
+            args, kw = self._ctor
+            self._twin_plan = IteratedSmootherPlan(*args, **kw)
+        plan = self if self._flip == 0 else self._twin_plan
+        done, copied = self._events[self._flip]
+        main = torch.cuda.current_stream(dev)
+        main.wait_event(copied)          # this plan's outputs of two calls ago have been read
+        plan.set_observations(ys_host)
+        plan.run()
+        done.record(main)
+        self._copy_stream.wait_event(done)
+        with torch.cuda.stream(self._copy_stream):
+            out_mean_host.copy_(plan.mean, non_blocking=True)
+            if out_chol_host is not None:
+                out_chol_host.copy_(plan.chol, non_blocking=True)
+        copied.record(self._copy_stream)
+        self._flip ^= 1
         return out_mean_host, out_chol_host
+
+    def sync_host(self):
+        """Make the current stream wait for the pipelined copy-outs."""
+        if self._copy_stream is not None:
+            torch.cuda.current_stream(self._args[0].device).wait_stream(self._copy_stream)
 
     def result(self):
         """The smoothed trajectory in the caller's layout."""

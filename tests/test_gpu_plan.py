@@ -72,3 +72,41 @@ def test_plan_replay_and_host_path():
     torch.cuda.synchronize()
     assert not torch.equal(plan.mean, first)
     assert torch.isfinite(plan.mean).all()
+
+
+def test_pipelined_host_path_matches():
+    """run_host(pipelined=True) alternates the plan with a twin and copies out on a second
+    stream; every call still returns that call's smoothed trajectory."""
+    ys, offsets, x0, tm, om, nom = _setup(torch.float32)
+    plan = S.IteratedSmootherPlan(ys, x0, tm, om, S.linearization.cubature, nom, criterion=S.FixedIterations(3),
+                                  offsets=offsets, streams=2)
+    ys_host = ys.clone().pin_memory()
+    m_ref = torch.empty(plan.mean.shape, dtype=torch.float32).pin_memory()
+    L_ref = torch.empty(plan.chol.shape, dtype=torch.float32).pin_memory()
+    plan.run_host(ys_host, m_ref, L_ref)
+    torch.cuda.synchronize()
+    outs = []
+    for k in range(4):
+        yk = ys_host.clone()
+        yk[:, 0] += 0.001 * k
+        yk = yk.pin_memory()
+        m_host = torch.empty_like(m_ref).pin_memory()
+        L_host = torch.empty_like(L_ref).pin_memory()
+        plan.run_host(yk, m_host, L_host, pipelined=True)
+        outs.append((m_host, L_host))
+    plan.sync_host()
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0][0], m_ref) and torch.equal(outs[0][1], L_ref)
+    for k in range(1, 4):
+        assert not torch.equal(outs[k][0], outs[k - 1][0])       # each call saw its own observations
+    # the twin plan (odd calls) computes what the plan itself computes
+    plan.run_host(ys_host, m_ref, L_ref)
+    torch.cuda.synchronize()
+    m_twin = torch.empty_like(m_ref).pin_memory()
+    L_twin = torch.empty_like(L_ref).pin_memory()
+    if plan._flip == 0:
+        plan.run_host(ys_host, torch.empty_like(m_ref).pin_memory(), None, pipelined=True)
+    plan.run_host(ys_host, m_twin, L_twin, pipelined=True)
+    plan.sync_host()
+    torch.cuda.synchronize()
+    assert torch.equal(m_twin, m_ref) and torch.equal(L_twin, L_ref)
