@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -149,6 +150,15 @@ static std::vector<ProfRec> g_prof;
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 bool profiling_on() { return g_profiling.load(std::memory_order_relaxed); }
+// Programmatic dependent launch of the per-pass kernels: on unless the
+// environment sets SQRTSMOOTH_PDL=0 (read once).
+bool pdl_on() {
+  static const bool on = [] {
+    const char* v = std::getenv("SQRTSMOOTH_PDL");
+    return !(v != nullptr && v[0] == '0');
+  }();
+  return on;
+}
 void profile_push(const char* name, cudaEvent_t start, cudaEvent_t stop) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof.push_back({name, start, stop});

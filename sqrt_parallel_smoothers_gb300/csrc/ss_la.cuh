@@ -59,6 +59,24 @@ SS_DEV void reflector(float x0, float sigma, float& beta, float& v0, float& k) {
   }
 }
 
+// Programmatic dependent launch (sm_90 and later).  The per-pass kernels are
+// launched with programmatic stream serialisation, so a kernel's launch is
+// prepared while its predecessor on the stream drains.  Each such kernel calls
+// pdl_enter() first: griddepcontrol.wait blocks until the predecessor has
+// completed and its writes are visible (a no-op without a programmatic
+// predecessor).  Every kernel of the chain waits before it completes, so a
+// kernel also sees the writes of all earlier kernels on its stream.  An early
+// launch_dependents (SS_PDL_TRIGGER=1) lets the successor's blocks take SM
+// slots while they wait; measured, that is 8 % slower than the trigger at
+// block exit, which is the default.
+#ifndef SS_PDL_TRIGGER
+#define SS_PDL_TRIGGER 0
+#endif
+SS_DEV void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (SS_PDL_TRIGGER) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // tria: on return M[:, :ROWS] holds the lower-triangular L (diag >= 0) with
 // L L^T = M M^T (input M), and M[:, ROWS:] is zero.  Householder reflections

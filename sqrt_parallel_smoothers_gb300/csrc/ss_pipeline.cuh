@@ -503,6 +503,7 @@ __global__ void __launch_bounds__(128) filter_leaf_kernel(ScanArgs<R> a) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) filter_up_kernel(ScanArgs<R> a, int l) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.g.lvl[l + 1][a.g.B]) return;
@@ -532,6 +533,7 @@ SS_DEV void load_prior(const ScanArgs<R>& a, int64_t i, State<R, NX>& s) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) filter_top_kernel(ScanArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.g.B) return;
@@ -557,6 +559,7 @@ __global__ void __launch_bounds__(128) filter_top_kernel(ScanArgs<R> a) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) filter_down_kernel(ScanArgs<R> a, int l) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.g.lvl[l + 1][a.g.B]) return;
@@ -650,6 +653,7 @@ __global__ void __launch_bounds__(128) smoother_leaf_kernel(ScanArgs<R> a) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) smoother_up_kernel(ScanArgs<R> a, int l) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.g.lvl[l + 1][a.g.B]) return;
@@ -703,6 +707,7 @@ SS_DEV void copy_state(const ScanArgs<R>& a, int64_t s) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) smoother_top_kernel(ScanArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.g.B) return;
@@ -730,6 +735,7 @@ __global__ void __launch_bounds__(128) smoother_top_kernel(ScanArgs<R> a) {
 
 template <typename R, int NX>
 __global__ void __launch_bounds__(128) smoother_down_kernel(ScanArgs<R> a, int l) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.g.lvl[l + 1][a.g.B]) return;
@@ -867,6 +873,7 @@ static __global__ void ll_reduce_kernel(Geo g, int ny, int NC, const double* __r
 // sequences whose mean squared change is <= tol, reset the accumulator.
 static __global__ void converge_kernel(Geo g, int nx, double tol, double* mse, int32_t* active,
                                 int32_t* iters) {
+  pdl_enter();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= g.B) return;
   if (active[i]) {

@@ -175,6 +175,25 @@ inline void record_event(cudaEvent_t e, cudaStream_t st) {
     }                                                                      \
   } while (0)
 
+// Launch with programmatic stream serialisation (the kernel must begin with
+// pdl_enter()), or plainly when that is switched off (SQRTSMOOTH_PDL=0).
+bool pdl_on();
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), unsigned grid, int block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_on() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // The scan-level kernels (up, top, down) have few, long-running items; one warp
 // per block spreads them over every SM.
 constexpr int LEVEL_BLOCK = 32;
@@ -188,7 +207,7 @@ inline int launch_lin_one(const LinArgs<R>& a, cudaStream_t st) {
   if constexpr (Vec16<R>::vec) {
     constexpr int sm = (int)StagedSmem<R, NX, NY>::lin;
     cudaFuncSetAttribute(lin_staged_kernel<R, NX, NY, TF, OF, METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    SS_LAUNCH("lin", st, lin_staged_kernel<R, NX, NY, TF, OF, METHOD><<<grid, STAGED_BLOCK, sm, st>>>(a));
+    SS_LAUNCH("lin", st, launch_pdl(lin_staged_kernel<R, NX, NY, TF, OF, METHOD>, grid, STAGED_BLOCK, sm, st, a));
   } else {
     SS_LAUNCH("lin", st, lin_kernel<R, NX, NY, TF, OF, METHOD><<<grid, 128, 0, st>>>(a));
   }
@@ -359,11 +378,11 @@ struct Runner {
   // Filter scan: level-1 summaries must already be in fsum[1] (filter_leaf).
   int filter_scan() {
     for (int l = 1; l < y.L; ++l) {
-      SS_LAUNCH("filter_up", st, filter_up_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
+      SS_LAUNCH("filter_up", st, launch_pdl(filter_up_kernel<R, NX>, grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa, l));
     }
-    SS_LAUNCH("filter_top", st, filter_top_kernel<R, NX><<<grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa));
+    SS_LAUNCH("filter_top", st, launch_pdl(filter_top_kernel<R, NX>, grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      SS_LAUNCH("filter_down", st, filter_down_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
+      SS_LAUNCH("filter_down", st, launch_pdl(filter_down_kernel<R, NX>, grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa, l));
     }
     return SS_OK;
   }
@@ -373,7 +392,7 @@ struct Runner {
     if constexpr (Vec16<R>::vec) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::leaf;
       cudaFuncSetAttribute(filter_leaf_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-      SS_LAUNCH("filter_leaf", st, filter_leaf_staged_kernel<R, NX, NY><<<g1, STAGED_BLOCK, sm, st>>>(sa));
+      SS_LAUNCH("filter_leaf", st, launch_pdl(filter_leaf_staged_kernel<R, NX, NY>, g1, STAGED_BLOCK, sm, st, sa));
     } else {
       SS_LAUNCH("filter_leaf", st, filter_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     }
@@ -383,7 +402,7 @@ struct Runner {
     if constexpr (Vec16<R>::vec) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::fwalk;
       cudaFuncSetAttribute(filter_walk_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-      SS_LAUNCH("filter_walk", st, filter_walk_staged_kernel<R, NX, NY><<<g1, STAGED_BLOCK, sm, st>>>(sa));
+      SS_LAUNCH("filter_walk", st, launch_pdl(filter_walk_staged_kernel<R, NX, NY>, g1, STAGED_BLOCK, sm, st, sa));
     } else {
       SS_LAUNCH("filter_walk", st, filter_walk_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     }
@@ -392,17 +411,17 @@ struct Runner {
 
   int smoother_scan_and_walk() {
     for (int l = 1; l < y.L; ++l) {
-      SS_LAUNCH("smoother_up", st, smoother_up_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
+      SS_LAUNCH("smoother_up", st, launch_pdl(smoother_up_kernel<R, NX>, grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa, l));
     }
-    SS_LAUNCH("smoother_top", st, smoother_top_kernel<R, NX><<<grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa));
+    SS_LAUNCH("smoother_top", st, launch_pdl(smoother_top_kernel<R, NX>, grid_for(p.batch, LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa));
     for (int l = y.L - 1; l >= 1; --l) {
-      SS_LAUNCH("smoother_down", st, smoother_down_kernel<R, NX><<<grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st>>>(sa, l));
+      SS_LAUNCH("smoother_down", st, launch_pdl(smoother_down_kernel<R, NX>, grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa, l));
     }
     if constexpr (Vec16<R>::vec) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::swalk;
       cudaFuncSetAttribute(smoother_walk_staged_kernel<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       SS_LAUNCH("smoother_walk", st,
-                smoother_walk_staged_kernel<R, NX><<<grid_for(y.items[1], STAGED_BLOCK), STAGED_BLOCK, sm, st>>>(sa));
+                launch_pdl(smoother_walk_staged_kernel<R, NX>, grid_for(y.items[1], STAGED_BLOCK), STAGED_BLOCK, sm, st, sa));
     } else {
       SS_LAUNCH("smoother_walk", st, smoother_walk_kernel<R, NX><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     }
@@ -506,7 +525,7 @@ struct Runner {
       rc = smoother_scan_and_walk();
       if (rc) return rc;
       if (tol_mode && counted) {
-        SS_LAUNCH("converge", st, converge_kernel<<<grid_for(p.batch, 128), 128, 0, st>>>(geo, NX, c.tol, mse, active, iters));
+        SS_LAUNCH("converge", st, launch_pdl(converge_kernel, grid_for(p.batch, 128), 128, 0, st, geo, NX, c.tol, mse, active, iters));
       }
       cur_m = om;
       cur_L = oL;

@@ -83,6 +83,7 @@ SS_DEV R* warp_smem(unsigned char* raw, size_t warp_elems) {
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY, class TF, class OF, int METHOD>
 __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(LinArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, NY> Q;
   extern __shared__ __align__(16) unsigned char ss_smem[];
   R* tile = warp_smem<R>(ss_smem, StageTile<R, Q::LIN>::WARP_ELEMS);
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(L
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY>
 __global__ void __launch_bounds__(STAGED_BLOCK, SS_LEAF_MINB) filter_leaf_staged_kernel(ScanArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, NY> Q;
   typedef StageTile<R, Q::LIN> TL;
   extern __shared__ __align__(16) unsigned char ss_smem[];
@@ -181,6 +183,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_LEAF_MINB) filter_leaf_staged
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY>
 __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged_kernel(ScanArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, NY> Q;
   typedef StageTile<R, Q::LIN> TL;
   typedef StageTile<R, Q::SE> TS;
@@ -284,6 +287,7 @@ __global__ void __launch_bounds__(STAGED_BLOCK, SS_SCAN_MINB) filter_walk_staged
 // ---------------------------------------------------------------------------
 template <typename R, int NX>
 __global__ void __launch_bounds__(STAGED_BLOCK, SS_SWALK_MINB) smoother_walk_staged_kernel(ScanArgs<R> a) {
+  pdl_enter();
   typedef Rec<R, NX, 1> Q;
   typedef StageTile<R, Q::SE> TS;
   constexpr int LW = StagedSmem<R, NX, 1>::out_stride;
