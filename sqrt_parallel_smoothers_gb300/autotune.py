@@ -14,8 +14,8 @@ import os
 import torch
 
 # (steps per chunk C, summaries per group G, concurrent sequence groups S)
-DEFAULT_CANDIDATES = ((8, 8, 1), (16, 4, 1), (32, 2, 1), (32, 4, 1), (32, 4, 3), (16, 8, 4), (8, 8, 4),
-                      (12, 4, 4), (16, 4, 2), (16, 4, 4), (16, 4, 6), (24, 4, 2), (24, 4, 4))
+DEFAULT_CANDIDATES = ((8, 8, 1), (16, 4, 1), (32, 4, 1), (32, 4, 3), (16, 8, 4), (8, 8, 4), (12, 4, 2),
+                      (12, 4, 4), (16, 4, 2), (16, 4, 3), (16, 4, 4), (20, 4, 2), (24, 4, 2), (24, 4, 4))
 
 
 def cache_path():

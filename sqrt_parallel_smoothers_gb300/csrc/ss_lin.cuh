@@ -101,9 +101,12 @@ SS_DEV void linearize_symmetric(const Fn& f, const R (&m)[DIN], const R (&C)[DIN
     R xp[DIN], xn[DIN];
     SS_UNROLL
     for (int i = 0; i < DIN; ++i) {
-      const R d = (i >= j) ? sc * C[i][j] : R(0);
-      xp[i] = m[i] + d;
-      xn[i] = m[i] - d;
+      // C is lower triangular: coordinates above column j stay exactly at the mean,
+      // so model outputs that depend only on those coordinates are shared by the
+      // points (the compiler evaluates them once)
+      const R d = sc * C[i][j];
+      xp[i] = (i >= j) ? m[i] + d : m[i];
+      xn[i] = (i >= j) ? m[i] - d : m[i];
     }
     f.eval(xp, fp[j]);
     f.eval(xn, fn[j]);
