@@ -13,12 +13,20 @@ namespace ss {
 
 constexpr int STAGED_BLOCK = 128;
 // Minimum resident blocks per SM requested from the register allocator for the
-// per-step kernels.  The smoother walk fits three blocks without spilling and the
-// linearisation with a few words of spill; the filter leaf and walk hold a
-// 2nx x 2nx tria and would spill heavily below 255 registers.
+// per-step kernels, each chosen by measurement: the FP32 linearisation runs four
+// blocks (128 registers, a few words of spill, 12 % faster than three; FP64
+// two, where three would spill 0.8 kB), the
+// smoother walk three, the filter leaf and walk one (they hold a 2nx x 2nx tria
+// and lose more to spills than they gain in occupancy).
 #ifndef SS_LIN_MINB
-#define SS_LIN_MINB 3
+#define SS_LIN_MINB 4
 #endif
+#ifndef SS_LIN_MINB_F64
+#define SS_LIN_MINB_F64 2
+#endif
+// FP64 registers come in pairs: its linearisation keeps fewer blocks
+template <typename R>
+struct LinMinBlocks { static constexpr int value = sizeof(R) == 4 ? SS_LIN_MINB : SS_LIN_MINB_F64; };
 #ifndef SS_SWALK_MINB
 #define SS_SWALK_MINB 3
 #endif
@@ -63,10 +71,12 @@ struct StagedSmem {
   static constexpr size_t lin = sizeof(R) * STAGED_WARPS * StageTile<R, Q::LIN>::WARP_ELEMS;
   static constexpr size_t leaf = 2 * lin;
   // the filter walk keeps each thread's chunk smoothing summary in shared
-  // memory (FP32), one column per thread
-  static constexpr bool walk_acc_smem = SS_WALK_ACC_SMEM && sizeof(R) == 4;
-  static constexpr size_t walk_acc = walk_acc_smem ? sizeof(R) * STAGED_BLOCK * Q::SE : 0;
-  static constexpr size_t fwalk = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS + walk_acc;
+  // memory, one column per thread, when that fits a block's 227 KB
+  static constexpr size_t fwalk_tiles = 2 * lin + sizeof(R) * STAGED_WARPS * StageTile<R, Q::SE>::WARP_ELEMS;
+  static constexpr size_t walk_acc_bytes = sizeof(R) * STAGED_BLOCK * Q::SE;
+  static constexpr bool walk_acc_smem = SS_WALK_ACC_SMEM && fwalk_tiles + walk_acc_bytes <= 232448;
+  static constexpr size_t walk_acc = walk_acc_smem ? walk_acc_bytes : 0;
+  static constexpr size_t fwalk = fwalk_tiles + walk_acc;
   // the smoother walk's output tile: a row holds nx x nx words (the caller's
   // layout) or one packed state record
   static constexpr int out_stride = ((NX * NX) | 1) > StageTile<R, Q::ST>::STRIDE ? ((NX * NX) | 1)
@@ -82,7 +92,7 @@ SS_DEV R* warp_smem(unsigned char* raw, size_t warp_elems) {
 
 // ---------------------------------------------------------------------------
 template <typename R, int NX, int NY, class TF, class OF, int METHOD>
-__global__ void __launch_bounds__(STAGED_BLOCK, SS_LIN_MINB) lin_staged_kernel(LinArgs<R> a) {
+__global__ void __launch_bounds__(STAGED_BLOCK, LinMinBlocks<R>::value) lin_staged_kernel(LinArgs<R> a) {
   pdl_enter();
   typedef Rec<R, NX, NY> Q;
   extern __shared__ __align__(16) unsigned char ss_smem[];
