@@ -125,10 +125,21 @@ SS_DEV void store_lin(R* p, const Lin<R, NX, NY>& l) {
 }
 
 template <typename R, int NX>
-SS_DEV void load_fe(const R* p, FElem<R, NX>& e) {
+SS_DEV void pack_fe(R (&r)[Rec<R, NX, 1>::FE_P], const FElem<R, NX>& e) {
   typedef Rec<R, NX, 1> Q;
-  R r[Q::FE_P];
-  load_rec<R, Q::FE>(p, r);
+  int o = 0;
+  pack<R, NX, NX>(r, o, e.A); o += NX * NX;
+  pack_vec<R, NX>(r, o, e.b); o += NX;
+  pack_tri<R, NX>(r, o, e.U); o += Q::TX;
+  pack_vec<R, NX>(r, o, e.eta); o += NX;
+  pack<R, NX, NX>(r, o, e.Z); o += NX * NX;
+  SS_UNROLL
+  for (int k = Q::FE; k < Q::FE_P; ++k) r[k] = R(0);
+}
+
+template <typename R, int NX>
+SS_DEV void unpack_fe(const R (&r)[Rec<R, NX, 1>::FE_P], FElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
   int o = 0;
   unpack<R, NX, NX>(r, o, e.A); o += NX * NX;
   unpack_vec<R, NX>(r, o, e.b); o += NX;
@@ -138,17 +149,18 @@ SS_DEV void load_fe(const R* p, FElem<R, NX>& e) {
 }
 
 template <typename R, int NX>
+SS_DEV void load_fe(const R* p, FElem<R, NX>& e) {
+  typedef Rec<R, NX, 1> Q;
+  R r[Q::FE_P];
+  load_rec<R, Q::FE>(p, r);
+  unpack_fe<R, NX>(r, e);
+}
+
+template <typename R, int NX>
 SS_DEV void store_fe(R* p, const FElem<R, NX>& e) {
   typedef Rec<R, NX, 1> Q;
   R r[Q::FE_P];
-  int o = 0;
-  pack<R, NX, NX>(r, o, e.A); o += NX * NX;
-  pack_vec<R, NX>(r, o, e.b); o += NX;
-  pack_tri<R, NX>(r, o, e.U); o += Q::TX;
-  pack_vec<R, NX>(r, o, e.eta); o += NX;
-  pack<R, NX, NX>(r, o, e.Z); o += NX * NX;
-  SS_UNROLL
-  for (int k = Q::FE; k < Q::FE_P; ++k) r[k] = R(0);
+  pack_fe<R, NX>(r, e);
   store_rec<R, Q::FE>(p, r);
 }
 
