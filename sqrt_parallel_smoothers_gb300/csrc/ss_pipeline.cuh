@@ -6,8 +6,9 @@
 // levels):
 //   lin_kernel        thread per step: linearise transition at nominal[t] and
 //                     observation at nominal[t+1] -> per-step Lin record
-//   filter_leaf       level-1 item: build the chunk's filtering elements and
-//                     fold them into one summary
+//   filter_leaf       level-1 item: the chunk's filtering summary (its first
+//                     step's element, extended one conditional Kalman step at
+//                     a time: filter_extend)
 //   filter_up         level l -> l+1 summaries (fold of G summaries)
 //   filter_top        one thread per sequence: walk the top level from the
 //                     prior, writing the state that enters each item

@@ -1,6 +1,6 @@
 // The four per-step kernels of the filter-smoother pass with their global
 // traffic staged through shared memory (see ss_stage.cuh): the per-step
-// linearisation, the chunk fold of filtering elements, the chunk Kalman walk
+// linearisation, the chunk's filtering summary, the chunk Kalman walk
 // and the chunk RTS walk.  Used for float and double; the per-lane variants
 // in ss_pipeline.cuh remain for dual numbers.
 #pragma once
