@@ -241,7 +241,7 @@ ALG_BYTES_PER_STEP = {
 }
 # DRAM bytes (read + write) per timestep of each kernel, from one ncu capture of this workload
 # (profiles/staged_kernels_bearings_b1024_c16g4.md: bytes of one launch / 1,101,870 timesteps)
-TRAFFIC_BYTES_PER_STEP = {"lin": 308, "filter_leaf": 268, "filter_walk": 426, "smoother_walk": 257}
+TRAFFIC_BYTES_PER_STEP = {"lin": 314, "filter_leaf": 269, "filter_walk": 426, "smoother_walk": 257}
 
 
 def adjoint_section(torch, S, flush):
