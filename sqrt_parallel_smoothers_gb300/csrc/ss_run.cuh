@@ -120,10 +120,13 @@ inline int make_layout(const ss_problem& p, Layout& y) {
   y.active = take(sizeof(int32_t) * (size_t)B);
   y.iters = take(sizeof(int32_t) * (size_t)B);
   const size_t S = (size_t)(N + B);
+  // The factor buffers also hold the loop's intermediate nominals as packed
+  // state records (run_iterated), which for nx <= 3 are longer than nx * nx.
+  constexpr size_t NOM_L = (size_t)(NX * NX > Q::ST_P ? NX * NX : Q::ST_P);
   y.nomA_m = take(sizeof(R) * S * NX);
-  y.nomA_L = take(sizeof(R) * S * NX * NX);
+  y.nomA_L = take(sizeof(R) * S * NOM_L);
   y.nomB_m = take(sizeof(R) * S * NX);
-  y.nomB_L = take(sizeof(R) * S * NX * NX);
+  y.nomB_L = take(sizeof(R) * S * NOM_L);
   y.bytes = o;
   return SS_OK;
 }
