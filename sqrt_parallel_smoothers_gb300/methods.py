@@ -787,6 +787,24 @@ def _dummy_transition(nx, dtype, device):
 
 # ----------------------------------------------------------------------------- graph-replayed plans
 
+def _group_cuts(lengths, k):
+    """Sequence boundaries [0 = c_0 < c_1 < ... = B] of at most k contiguous groups with about
+    equal numbers of steps, every group holding at least one step (when any sequence has one)."""
+    lengths = np.asarray(lengths, dtype=np.int64)
+    B = len(lengths)
+    off = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    k = max(1, min(int(k), B))
+    cuts = [0]
+    for g in range(1, k):
+        c = int(np.searchsorted(off, g * off[-1] / k))
+        cuts.append(max(cuts[-1] + 1, min(c, B - (k - g))))
+    cuts.append(B)
+    cuts = [c for i, c in enumerate(cuts) if i == 0 or off[c] > off[cuts[i - 1]] or c == B]
+    if len(cuts) > 2 and off[cuts[-1]] == off[cuts[-2]]:
+        del cuts[-2]
+    return cuts
+
+
 class IteratedSmootherPlan:
     """An iterated smoother staged once and replayed as a CUDA graph.
 
@@ -867,15 +885,7 @@ class IteratedSmootherPlan:
         (ys, offsets, m0, L0, im, iL, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg) = self._args
         lay, nx, dev = self.layout, self.nx, ys.device
         off = np.concatenate([[0], np.cumsum(lay.lengths)]).astype(np.int64)
-        k = min(k, lay.B)
-        cuts = [0]
-        for g in range(1, k):          # about equal steps per group, no group empty
-            c = int(np.searchsorted(off, g * off[-1] / k))
-            cuts.append(max(cuts[-1] + 1, min(c, lay.B - (k - g))))
-        cuts.append(lay.B)
-        cuts = [c for i, c in enumerate(cuts) if i == 0 or off[c] > off[cuts[i - 1]] or c == lay.B]
-        if len(cuts) > 2 and off[cuts[-1]] == off[cuts[-2]]:
-            del cuts[-2]                 # every group holds at least one step
+        cuts = _group_cuts(lay.lengths, k)
         per, want_ell, n_iter, tol = icfg[13], icfg[14], icfg[15], fcfg[11]
         N, B = lay.N, lay.B
         out_m = torch.empty((N + B, nx), dtype=ys.dtype, device=dev)

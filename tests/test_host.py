@@ -155,3 +155,23 @@ def test_gh_roots_match_numpy():
         from oracle.linearization import gauss_hermite_weights
         wm, _, xi = gauss_hermite_weights(1, p)
         np.testing.assert_allclose(np.sort(xi[:, 0]), np.sqrt(2) * np.sort(r), atol=1e-10)
+
+
+def test_group_cuts_cover_the_batch():
+    """Concurrent sequence groups of IteratedSmootherPlan: contiguous, covering every sequence,
+    at most k of them, each with at least one step, about equal in steps."""
+    rng = np.random.RandomState(0)
+    cases = [np.array([60, 3, 0, 140, 97, 1, 33, 250]), np.array([0, 0, 5, 0]), np.array([5, 0, 0, 0]),
+             np.array([1, 1]), np.array([7]), rng.randint(0, 50, size=300)]
+    for lengths in cases:
+        off = np.concatenate([[0], np.cumsum(lengths)])
+        for k in (1, 2, 3, 4, 6, 8):
+            cuts = methods._group_cuts(lengths, k)
+            assert cuts[0] == 0 and cuts[-1] == len(lengths)
+            assert all(a < b for a, b in zip(cuts[:-1], cuts[1:]))
+            assert len(cuts) - 1 <= k
+            steps = [int(off[b] - off[a]) for a, b in zip(cuts[:-1], cuts[1:])]
+            if off[-1] > 0:
+                assert min(steps) >= 1
+            if len(lengths) >= 100 and k > 1:
+                assert max(steps) <= 2 * off[-1] / (len(cuts) - 1)
