@@ -3,12 +3,16 @@
 Workload (the batched configuration): B = 1024 independent bearings-only
 sequences (coordinated-turn state, two bearings sensors, dt = 0.01), lengths
 drawn log-uniform in [50, 5000] (seed 0), sequence i simulated from seed i
-(+ 1024 * rank), iterated square-root cubature smoother started the
-reference's default way (one filter-smoother pass at zero means / identity
-factors) followed by 10 filter-smoother calls, FP32.  One step = the
-whole 10-call smoother over the batch, replayed from one CUDA graph.
-``value`` = sum_i T_i / device time of a step (inputs resident).  The FP64
-plain path (B = 1, T = 5000, FP64, same method) is timed beside it.
+(+ 1024 * rank), iterated square-root cubature smoother: 10 filter-smoother
+calls from the prior mean broadcast, FP32.  One step = the whole 10-call
+smoother over the batch, replayed from one CUDA graph at the scan geometry
+and number of concurrent sequence groups the autotuner picks.  ``value`` =
+sum_i T_i / device time of a step (inputs resident, L2 flushed between
+steps); ``e2e`` = the same through ``IteratedSmootherPlan.run_host`` with
+pinned host observations in and the smoothed trajectory out every step
+(copy-out overlapped with the next step).  The FP64 plain path (B = 1,
+T = 5000, FP64, same method) is timed beside it, and the per-kernel times
+for the roofline come from a single-stream replay of the same geometry.
 
 ``--impl reference`` times the reference algorithm on the host CPU (the
 FP64 NumPy port in ``oracle/``: the reference's JAX code cannot be
