@@ -334,3 +334,52 @@ def test_filter_prefix_of_long_sequence(dtype, tol):
     assert_rel(filt.mean[:P + 1], ref.mean, tol, "filtered mean prefix")
     assert_rel(cov(filt.chol[:P + 1]), cov(ref.chol), tol, "filtered cov prefix")
     assert torch.isfinite(filt.mean).all()
+
+
+# ----------------------------------------------------------------------------- information limits
+
+@pytest.mark.parametrize("dim_x", [1, 3])
+@pytest.mark.parametrize("dim_y", [2, 3])
+@pytest.mark.parametrize("method", ["cubature", "extended"])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_filter_no_info_gpu(dim_x, dim_y, method, dtype):
+    """Observations with a huge noise (chol R x 1e6) carry no information: the filter is the
+    prediction (the reference's tests/test_sequential_filter.py limit case), and the GPU
+    matches the oracle in that regime."""
+    from tests._systems import get_system
+    np.random.seed(3)
+    x0, chol_x0, F, Q, cholQ, b, _ = get_system(dim_x, dim_x)
+    _, _, H, R, cholR, c, _ = get_system(dim_x, dim_y)
+    cholR = 1e6 * cholR
+    ys = np.random.randn(3, dim_y)
+    ot, gt = linear_pair(F, b, cholQ)
+    oo, go = linear_pair(H, c, cholR)
+    expected = [x0.mean]
+    for _ in range(3):
+        expected.append(F @ expected[-1] + b)
+    ref = O.methods.filtering(ys, chol_x0, ot, oo, ORACLE_LIN[method], None, True)
+    res = S.filtering(torch.as_tensor(ys, dtype=dtype), S.MVNSqrt(torch.as_tensor(chol_x0.mean),
+                      torch.as_tensor(chol_x0.chol)), gt, go, GPU_LIN[method], None)
+    np.testing.assert_allclose(np_(res.mean), np.asarray(expected), atol=1e-3, rtol=1e-3)
+    assert_rel(res.mean, ref.mean, 1e-9 if dtype == torch.float64 else 1e-4, "mean vs oracle")
+
+
+@pytest.mark.parametrize("dim", [1, 3])
+@pytest.mark.parametrize("method", ["cubature", "extended"])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_filter_infinite_info_gpu(dim, method, dtype):
+    """Near-noiseless identity observations (chol R x 1e-3): the filtered means follow
+    y - c (the reference's infinite-information limit case)."""
+    from tests._systems import get_system
+    np.random.seed(4)
+    x0, chol_x0, _, Q, cholQ, b, _ = get_system(dim, dim)
+    _, _, _, R, cholR, c, _ = get_system(dim, dim)
+    cholR = 1e-3 * cholR
+    ys = np.random.randn(3, dim)
+    ot, gt = linear_pair(np.eye(dim), b, cholQ)
+    oo, go = linear_pair(np.eye(dim), c, cholR)
+    ref = O.methods.filtering(ys, chol_x0, ot, oo, ORACLE_LIN[method], None, True)
+    res = S.filtering(torch.as_tensor(ys, dtype=dtype), S.MVNSqrt(torch.as_tensor(chol_x0.mean),
+                      torch.as_tensor(chol_x0.chol)), gt, go, GPU_LIN[method], None)
+    np.testing.assert_allclose(np_(res.mean)[1:], ys - c, atol=1e-3, rtol=1e-3)
+    assert_rel(res.mean, ref.mean, 1e-9 if dtype == torch.float64 else 1e-4, "mean vs oracle")
