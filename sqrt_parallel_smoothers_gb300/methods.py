@@ -976,7 +976,9 @@ class IteratedSmootherPlan:
         (its own outputs and workspace, built at the first such call) and the
         copy-out runs on a separate stream, so one call's device-to-host copy
         overlaps the next call's smoother.  The host buffers are complete once
-        :meth:`sync_host` has been called (or the copy stream synchronised)."""
+        :meth:`sync_host` has been called (or the copy stream synchronised).
+        Pipelined results are delivered only to the host buffers: :attr:`mean`
+        and :attr:`chol` hold this plan's own last replay, not the twin's."""
         if not pipelined:
             self.set_observations(ys_host)
             self.run()
