@@ -175,3 +175,21 @@ def test_group_cuts_cover_the_batch():
                 assert min(steps) >= 1
             if len(lengths) >= 100 and k > 1:
                 assert max(steps) <= 2 * off[-1] / (len(cuts) - 1)
+
+
+def test_layout_rejects_bad_shapes():
+    """Shape errors are raised on the host, before any device work (ValueError, as the
+    reference's own shape checks)."""
+    ys = torch.zeros(3, 5, 2)
+    with pytest.raises(ValueError):
+        methods._Layout(ys, np.array([1, 2]), None, None, torch.device("cpu"))        # B mismatch
+    with pytest.raises(ValueError):
+        methods._Layout(ys, np.array([1, 6, 2]), None, None, torch.device("cpu"))     # T_i > T
+    with pytest.raises(ValueError):
+        methods._Layout(ys, np.array([1, -1, 2]), None, None, torch.device("cpu"))    # negative
+    with pytest.raises(ValueError):
+        methods._Layout(torch.zeros(3, 5, 2, 1), None, None, None, torch.device("cpu"))  # rank 4
+    with pytest.raises(ValueError):
+        methods._Layout(torch.zeros(10), None, [0, 4, 10], None, torch.device("cpu"))   # packed needs (N, ny)
+    with pytest.raises(TypeError):
+        methods._Layout(torch.zeros(4, 2, dtype=torch.int32), None, None, torch.int32, torch.device("cpu"))
