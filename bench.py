@@ -20,6 +20,7 @@ installed here) on a bounded sample of the same workload, with one process
 per host core.
 """
 import argparse
+import datetime
 import json
 import os
 import subprocess
@@ -65,7 +66,6 @@ def _oracle_task(args):
     Q, R = O.models.bearings_noise(QC, QW, SIGMA, DT)
     tm = O.FunctionalModel(O.models.CoordinatedTurn(DT), O.MVNSqrt(np.zeros(5), np.linalg.cholesky(Q)))
     om = O.FunctionalModel(O.models.Bearings(S1, S2), O.MVNSqrt(np.zeros(2), np.linalg.cholesky(R)))
-    T = ys.shape[0]
     T = ys.shape[0]
     nom = O.MVNSqrt(np.repeat(m0[None], T + 1, 0), np.repeat(np.eye(5)[None], T + 1, 0))
     res = O.methods.iterated_smoothing(ys.astype(np.float64), O.MVNSqrt(m0, np.eye(5)), tm, om,
@@ -135,54 +135,104 @@ def reference_arm(args):
 # ----------------------------------------------------------------------------- GPU arm
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every ``period_ms`` from before the
+    warm-up to the end of the timed region.  Each sample carries nvidia-smi's own timestamp
+    (so pipe buffering does not matter); :meth:`stop` keeps the samples taken inside the timed
+    window ``[t0, t1]`` (``window: "timed"``) or, when the window is shorter than the sampling
+    period and holds none, the last sample before ``t1`` (``window: "nearest"``, taken under the
+    warm-up's load of the same work)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_ms=25, exe="nvidia-smi"):
         self.gpu = gpu_index
+        self.period_ms = int(period_ms)
+        self.exe = exe
+        self.fields = self.FIELDS + ",timestamp"
         self.proc = None
-        self.lines = []
+        self.lines = []                  # (host arrival time, line)
 
-    def start(self):
+    def _spawn(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+            self.proc = subprocess.Popen([self.exe, f"--id={self.gpu}", f"--query-gpu={self.fields}",
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
         except OSError:
             self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, args=(self.proc,), daemon=True)
+        self.thread.start()
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
+    def start(self, first_line_timeout=2.0):
+        """Start sampling; return once the first sample has arrived, nvidia-smi has exited or
+        the timeout has passed.  If nvidia-smi exits without a sample (an interval or a field
+        it does not take), sample again every 200 ms without the timestamp field (the samples
+        are then stamped with their arrival time)."""
+        self._spawn()
+        if self.proc is None:
+            return
+        t_end = time.monotonic() + first_line_timeout
+        while not self.lines and self.proc.poll() is None and time.monotonic() < t_end:
+            time.sleep(0.005)
+        if not self.lines and self.proc.poll() is not None and self.period_ms < 200:
+            self.thread.join(timeout=5)
+            self.period_ms, self.fields = 200, self.FIELDS
+            self._spawn()
 
-    def stop(self):
+    def _read(self, proc):
+        for line in proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    @staticmethod
+    def _stamp(text, fallback):
+        try:
+            return datetime.datetime.strptime(text.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return fallback
+
+    def stop(self, t0=None, t1=None):
+        """Stop sampling and summarise the samples of the timed window ``[t0, t1]`` (host
+        ``time.time()`` values; every sample when they are not given)."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        if t1 is not None:
+            # let the sample that straddles t1 be taken
+            t_end = time.time() + self.period_ms / 1000.0
+            while time.time() < t_end and self.proc.poll() is None:
+                time.sleep(0.005)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        self.thread.join(timeout=5)
+        samples = []
+        for arrived, ln in list(self.lines):
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                sm, smax = float(parts[1]), float(parts[2])
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(nm)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+            t = self._stamp(parts[9], arrived) if len(parts) > 9 else arrived
+            samples.append((t, sm, smax, {nm for nm, v in zip(self.NAMES, parts[5:9])
+                                          if v.lower().startswith("active")}))
+        window = "all"
+        if t0 is not None and t1 is not None:
+            inside = [s for s in samples if t0 <= s[0] <= t1]
+            if inside:
+                samples, window = inside, "timed"
+            else:
+                before = [s for s in samples if s[0] <= t1]
+                samples, window = (before[-1:], "nearest") if before else (samples, "all")
+        sm = [s[1] for s in samples]
+        reasons = set().union(*[s[3] for s in samples]) if samples else set()
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(s[2] for s in samples) if samples else None,
+                "reasons": sorted(reasons), "samples": len(sm), "period_ms": self.period_ms, "window": window}
 
 
 def models(torch, S, dtype):
@@ -207,12 +257,13 @@ def make_plan(torch, S, ys, offsets, dtype, chunk=0, group=0, graph=True, profil
 
 
 def time_plan(torch, plan, steps, warmup, flush=None, sampler=None):
+    if sampler is not None:
+        sampler.start()
     for _ in range(warmup):
         plan.run()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    if sampler is not None:
-        sampler.start()
+    t0 = time.time()
     for k in range(steps):
         if flush is not None:
             flush.add_(1)
@@ -220,7 +271,8 @@ def time_plan(torch, plan, steps, warmup, flush=None, sampler=None):
         plan.run()
         ev[k][1].record()
     torch.cuda.synchronize()
-    clocks = sampler.stop() if sampler is not None else None
+    t1 = time.time()
+    clocks = sampler.stop(t0, t1) if sampler is not None else None
     return [a.elapsed_time(b) for a, b in ev], clocks
 
 
