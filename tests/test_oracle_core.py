@@ -101,3 +101,25 @@ def test_unscented_default_kappa():
     assert wm[0] == pytest.approx(lam / (2 + lam))
     assert wm.sum() == pytest.approx(1.0)
     np.testing.assert_allclose(xi.T @ (wc[:, None] * xi), np.eye(2), atol=1e-12)
+
+
+def test_fixed_point_known_answer():
+    # tests/test_math_utils.py:57-67 of the reference: x <- 0.7 x + 0.5 from 1 converges to 0.5 / 0.3
+    from oracle.methods import fixed_point
+    x, calls = fixed_point(lambda x: 0.7 * x + 0.5, 1.0, lambda i, *_: i < 500)
+    assert x == pytest.approx(0.5 / 0.3, rel=1e-7, abs=1e-7)
+    assert calls == 500
+
+
+@pytest.mark.parametrize("n", [1, 2, 10])
+def test_fixed_point_calls_f_n_times(n):
+    # parsmooth/_utils.py:136-146: the loop starts at (1, x0, f(x0)), so `i < n` makes n calls of f
+    from oracle.methods import fixed_point
+    seen = []
+
+    def f(x):
+        seen.append(x)
+        return x + 1
+
+    x, calls = fixed_point(f, 0, lambda i, *_: i < n)
+    assert len(seen) == n and calls == n and x == n
