@@ -61,5 +61,10 @@ def resolve(method):
 
 
 def get_conditional_model(*_args, **_kwargs):
-    """parsmooth/linearization/_common.py:17-66: conditional-moments models are not built."""
-    raise NotImplementedError("ConditionalMomentsModel is not supported by the GPU smoother")
+    """parsmooth/linearization/_common.py:17-66 turns a Python callable ``f(x, q)`` with
+    non-additive noise into conditional moments by linearising it in ``q`` at every point.  A
+    Python callable cannot run inside the CUDA kernels, so this raises
+    ``NotImplementedError``; a :class:`ConditionalMomentsModel` of device models
+    (``models.Ricker``, ``models.PoissonExp``, ``models.population_parameters``) is supported."""
+    raise NotImplementedError("get_conditional_model needs a Python callable f(x, q), which cannot run in the "
+                              "CUDA kernels; build a ConditionalMomentsModel from device models instead")

@@ -145,6 +145,9 @@ def test_ragged_layout_roundtrip():
 def test_non_device_models_are_rejected():
     with pytest.raises(NotImplementedError):
         S.models.as_device_model(lambda x: x)
+    # parsmooth/linearization/_common.py:17-66 wraps a Python f(x, q): no device form
+    with pytest.raises(NotImplementedError, match="device models"):
+        S.linearization.get_conditional_model(lambda x, q: x + q, None, S.linearization.cubature)
 
 
 def test_gh_roots_match_numpy():
