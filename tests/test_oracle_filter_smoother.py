@@ -1,6 +1,6 @@
 """Oracle filter/smoother relations (CPU), porting the reference's
-tests/test_parallel_operators.py:17-89, test_parallel_filter.py:76-122,
-test_parallel_smoother.py:57-99, test_iterated_smoother.py:26-69 and
+tests/test_parallel_operators.py:17-89, test_parallel_filter.py:26-122,
+test_parallel_smoother.py:26-99, test_iterated_smoother.py:26-69 and
 test_sequential_filter.py:120-184."""
 import numpy as np
 import pytest
@@ -148,3 +148,41 @@ def test_filter_infinite_info(dim, seed, lin):
     om = FunctionalModel(OM.LinearFunction(np.eye(dim)), MVNSqrt(c, cholR))
     res = P.filtering(ys, chol_x0, tm, om, lin, None)
     np.testing.assert_allclose(res.mean[1:], ys - c, atol=1e-3, rtol=1e-3)
+
+
+@pytest.mark.parametrize("dim_x", [1, 2, 3])
+@pytest.mark.parametrize("dim_y", [1, 2, 3])
+@pytest.mark.parametrize("seed", [0, 42])
+@pytest.mark.parametrize("lin", LINS, ids=lambda m: m.name)
+def test_elements_sqrt_vs_standard(dim_x, dim_y, seed, lin):
+    # tests/test_parallel_filter.py:26-75 and tests/test_parallel_smoother.py:26-55 of the
+    # reference: one step's filtering and smoothing elements at a nominal N(m, I) of a linear
+    # system, square-root against covariance form, and the linearised model is the system itself
+    np.random.seed(seed)
+    x0, chol_x0, F, Q, cholQ, b, _ = get_system(dim_x, dim_x)
+    _, _, H, R, cholR, c, _ = get_system(dim_x, dim_y)
+    m_nom = np.random.randn(dim_x)
+    y = np.random.randn(dim_y)
+    s = dict(F=F, H=H, Q=Q, R=R, cholQ=cholQ, cholR=cholR, b=b, c=c)
+    (tm_s, om_s), (tm, om) = _models(s, True), _models(s, False)
+    Fs, cQs, bs = lin(tm_s, MVNSqrt(m_nom, np.eye(dim_x)))
+    Hs, cRs, cs = lin(om_s, MVNSqrt(m_nom, np.eye(dim_x)))
+    Fc, Qc, bc = lin(tm, MVNStandard(m_nom, np.eye(dim_x)))
+    Hc, Rc, cc = lin(om, MVNStandard(m_nom, np.eye(dim_x)))
+    for got, want in ((Fs, F), (bs, b), (Hs, H), (cs, c), (cQs @ cQs.T, Q), (cRs @ cRs.T, R),
+                      (Fc, F), (bc, b), (Hc, H), (cc, c), (Qc, Q), (Rc, R)):
+        np.testing.assert_allclose(got, want, atol=1e-9)
+
+    A1, b1, U, eta1, Z = P.sqrt_filter_elements(Fs, cQs, bs, Hs, cRs, cs, y, chol_x0.mean, chol_x0.chol)
+    A2, b2, C, eta2, J = P.standard_filter_elements(Fc, Qc, bc, Hc, Rc, cc, y, x0.mean, x0.cov)
+    np.testing.assert_allclose(A1, A2, atol=1e-9)
+    np.testing.assert_allclose(b1, b2, atol=1e-9)
+    np.testing.assert_allclose(eta1, eta2, atol=1e-9)
+    np.testing.assert_allclose(U @ U.T, C, atol=1e-9)
+    np.testing.assert_allclose(Z @ Z.T, J, atol=1e-9)
+
+    g1, E1, D = P.sqrt_smoother_elements(Fs, cQs, bs, chol_x0.mean, chol_x0.chol)
+    g2, E2, L = P.standard_smoother_elements(Fc, Qc, bc, x0.mean, x0.cov)
+    np.testing.assert_allclose(g1, g2, atol=1e-9)
+    np.testing.assert_allclose(E1, E2, atol=1e-9)
+    np.testing.assert_allclose(D @ D.T, L, atol=1e-9)
