@@ -1,7 +1,7 @@
 """Oracle sequential steps (CPU): the square-root and covariance-form predict, update and RTS
 smoothing steps against their closed forms and against each other, porting the relations of
-the reference's tests/test_sequential_filter.py:24-118 and
-tests/test_sequential_smoother.py:24-121 (these steps are the sequential oracle the parallel
+the reference's tests/test_sequential_filter.py:24-250 and
+tests/test_sequential_smoother.py:24-200 (these steps are the sequential oracle the parallel
 path is checked against)."""
 import numpy as np
 import pytest
@@ -105,3 +105,35 @@ def test_smooth_one_with_infinite_process_noise(dim_x, seed):
     for mean, cov in ((m_s, _cov(L_s)), (m, P)):
         np.testing.assert_allclose(mean, xf.mean, atol=1e-5)
         np.testing.assert_allclose(cov, xf.cov, atol=1e-5)
+
+
+@pytest.mark.parametrize("dim_x", [1, 3])
+@pytest.mark.parametrize("dim_y", [2, 3])
+@pytest.mark.parametrize("seed", [0, 42])
+@pytest.mark.parametrize("with_nominal", [False, True])
+def test_all_filters_and_smoothers_agree(dim_x, dim_y, seed, with_nominal):
+    # tests/test_sequential_filter.py:186-250 and tests/test_sequential_smoother.py:123-200 of
+    # the reference: on a linear system the four linearisations, in square-root and covariance
+    # form, with or without a nominal trajectory, give one filter and one smoother
+    from oracle import linearization as LZ
+    from oracle.types import MVNSqrt, MVNStandard
+    from tests._systems import lgssm
+    from tests.test_oracle_filter_smoother import _models
+    T = 5
+    s = lgssm(dim_x, dim_y, T, seed)
+    means_f, means_s = [], []
+    for lin in (LZ.extended, LZ.cubature, LZ.gauss_hermite, LZ.unscented):
+        for sqrt in (True, False):
+            tm, om = _models(s, sqrt)
+            x0 = s["chol_x0"] if sqrt else s["x0"]
+            nom = None
+            if with_nominal:
+                eye = np.repeat(np.eye(dim_x)[None], T + 1, 0)
+                nom = (MVNSqrt if sqrt else MVNStandard)(s["m_nominal"], eye)
+            filt = S.filtering(s["ys"], x0, tm, om, lin, nom)
+            means_f.append(filt.mean)
+            means_s.append(S.smoothing(tm, filt, lin, nom).mean)
+    for got in means_f[1:]:
+        np.testing.assert_allclose(got, means_f[0], atol=1e-8)
+    for got in means_s[1:]:
+        np.testing.assert_allclose(got, means_s[0], atol=1e-8)
