@@ -24,7 +24,9 @@ class FunctionalModel(NamedTuple):
 
 
 class ConditionalMomentsModel(NamedTuple):
-    """Conditional-moments model (parsmooth/_base.py:20-22); not supported on the GPU path."""
+    """Conditional-moments model (parsmooth/_base.py:20-22).  On the GPU path both functions
+    must be the conditional moments of one device model (``models.Ricker``,
+    ``models.PoissonExp``, ``models.population_parameters``)."""
     conditional_mean: Callable
     conditional_covariance_or_cholesky: Callable
 

@@ -199,7 +199,10 @@ def _model_tensors(model, d_in, d_out, dtype, device, sqrt=True):
         raise ValueError(f"{fn!r} maps R^{fn.d_in} -> R^{fn.d_out}, expected R^{d_in} -> R^{d_out}")
     q = model.mvn
     if isinstance(q, MVNStandard):
-        raise NotImplementedError("covariance-form (MVNStandard) models are not supported: use MVNSqrt")
+        # covariance-form inputs were converted as a whole before this point, so this noise
+        # sits beside square-root inputs (parsmooth/linearization/_sigma_points.py:64 raises too)
+        raise TypeError(f"All inputs should have the same type: an MVNStandard noise with MVNSqrt states "
+                        f"({model!r})")
     qm = _as(q.mean, dtype, device).reshape(d_out)
     qL = _lower(_as(q.chol, dtype, device)).reshape(d_out, d_out).contiguous()
     mat = fn.matrix()
@@ -493,7 +496,8 @@ def _check_common(x0, parallel, method):
     if not parallel:
         raise NotImplementedError("only parallel=True is implemented on the GPU")
     if isinstance(x0, MVNStandard):
-        raise NotImplementedError("covariance-form (MVNStandard) inputs are not supported: use MVNSqrt")
+        raise NotImplementedError("this entry point takes square-root (MVNSqrt) inputs; filtering, smoothing, "
+                                  "sampling and iterated_smoothing also accept MVNStandard")
     if not isinstance(x0, MVNSqrt):
         raise TypeError(f"x0 must be an MVNSqrt, got {type(x0).__name__}")
     return resolve(method)
@@ -503,7 +507,8 @@ def _nominal(nominal, lay, nx):
     if nominal is None:
         return None, None
     if isinstance(nominal, MVNStandard):
-        raise NotImplementedError("covariance-form nominal trajectories are not supported")
+        raise TypeError("All inputs should have the same type: an MVNStandard nominal trajectory with an "
+                        "MVNSqrt prior")
     m = lay.pack_states(nominal.mean, (nx,))
     L = lay.pack_states(nominal.chol, (nx, nx))
     return m, _lower_batched(L)

@@ -196,3 +196,17 @@ def test_layout_rejects_bad_shapes():
         methods._Layout(torch.zeros(10), None, [0, 4, 10], None, torch.device("cpu"))   # packed needs (N, ny)
     with pytest.raises(TypeError):
         methods._Layout(torch.zeros(4, 2, dtype=torch.int32), None, None, torch.int32, torch.device("cpu"))
+
+
+def test_mixed_sqrt_and_covariance_inputs_raise_type_error():
+    # parsmooth/_base.py:25-30 via parsmooth/linearization/_sigma_points.py:64: a covariance-form
+    # noise or nominal beside square-root states is a TypeError, as in the reference
+    A = torch.eye(2, dtype=torch.float64)
+    model = S.FunctionalModel(S.models.LinearModel(A), S.MVNStandard(torch.zeros(2, dtype=torch.float64), A))
+    with pytest.raises(TypeError, match="same type"):
+        methods._model_tensors(model, 2, 2, torch.float64, torch.device("cpu"))
+    with pytest.raises(TypeError, match="same type"):
+        methods._nominal(S.MVNStandard(torch.zeros(3, 2), torch.eye(2).expand(3, 2, 2)), None, 2)
+    # the plan and the gradients take square-root inputs only, and say which entry points convert
+    with pytest.raises(NotImplementedError, match="iterated_smoothing also accept MVNStandard"):
+        methods._check_common(S.MVNStandard(torch.zeros(2), torch.eye(2)), True, cubature)
