@@ -210,3 +210,20 @@ def test_mixed_sqrt_and_covariance_inputs_raise_type_error():
     # the plan and the gradients take square-root inputs only, and say which entry points convert
     with pytest.raises(NotImplementedError, match="iterated_smoothing also accept MVNStandard"):
         methods._check_common(S.MVNStandard(torch.zeros(2), torch.eye(2)), True, cubature)
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason="checks the behaviour without a CUDA device")
+def test_no_cpu_fallback_without_a_gpu():
+    # every public entry point needs the CUDA path; none computes on the host instead
+    A = torch.eye(2, dtype=torch.float64)
+    noise = S.MVNSqrt(torch.zeros(2, dtype=torch.float64), A)
+    tm = om = S.FunctionalModel(S.models.LinearModel(A), noise)
+    x0 = S.MVNSqrt(torch.zeros(2, dtype=torch.float64), A)
+    ys = torch.zeros(4, 2, dtype=torch.float64)
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        S.filtering(ys, x0, tm, om, cubature)
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        S.iterated_smoothing(ys, x0, tm, om, cubature, criterion=lambda i, *_: i < 2)
+    with pytest.raises(RuntimeError, match="CUDA device"):
+        S.filtering(ys, S.MVNStandard(x0.mean, A), S.FunctionalModel(tm.function, S.MVNStandard(noise.mean, A)),
+                    S.FunctionalModel(om.function, S.MVNStandard(noise.mean, A)), cubature)
