@@ -539,8 +539,8 @@ def filtering(observations, x0, transition_model, observation_model, linearizati
     """Parallel square-root filter (parsmooth/methods.py:14-26 -> parsmooth/parallel/_filtering.py:13-61).
 
     Covariance-form inputs (``MVNStandard`` prior, nominal and model noises, the reference's
-    standard filter) are factored on the device, filtered by the square-root kernels and
-    returned as covariances."""
+    standard filter) are factored by torch where the tensors live (the GPU for CUDA inputs),
+    filtered by the square-root kernels and returned as covariances."""
     if isinstance(x0, MVNStandard):
         if nominal_trajectory is not None:
             are_inputs_compatible(x0, nominal_trajectory)
