@@ -47,7 +47,7 @@ def _robustness_ell(lin, T, run, ys):
     return ell
 
 
-@pytest.mark.parametrize("T", [20, 50, 100])
+@pytest.mark.parametrize("T", [20, 30, 40, 50, 80, 100])
 def test_robustness_loglikelihood_extended(T):
     d = np.load(os.path.join(GOLD, "robustness_small.npz"))
     ti = list(d["Ts"]).index(T)
