@@ -11,7 +11,8 @@ reference at run time.
   ``notebooks/robustness_data/data-T8000-Run*.npz`` and the FP32 GPU
   log-likelihoods the reference computed on them for T in 20..100
   (notebooks/robustness_100runs.py:46-69 and the saved
-  ``ell_float32_{cubature,extended}_sqrt_100runs.npz``).
+  ``ell_float32_{cubature,extended}_{sqrt,std}_100runs.npz``: square-root and
+  covariance form; NaN where the reference's FP32 run failed).
 """
 import os
 import shutil
@@ -34,8 +35,12 @@ def main():
         ell_cub = d["gpu_ICKS_sqrt_par_ell"][:len(Ts), :runs]
     with np.load(f"{base}/ell_float32_extended_sqrt_100runs.npz") as d:
         ell_ext = d["rts_gpu_IEKS_sqrt_par_ell"][:len(Ts), :runs]
+    with np.load(f"{base}/ell_float32_cubature_std_100runs.npz") as d:
+        ell_cub_std = d["gpu_ICKS_std_par_ell"][:len(Ts), :runs]
+    with np.load(f"{base}/ell_float32_extended_std_100runs.npz") as d:
+        ell_ext_std = d["rts_gpu_IEKS_std_par_ell"][:len(Ts), :runs]
     np.savez_compressed(f"{HERE}/robustness_small.npz", ys=ys, Ts=Ts, ell_cubature=ell_cub,
-                        ell_extended=ell_ext)
+                        ell_extended=ell_ext, ell_cubature_std=ell_cub_std, ell_extended_std=ell_ext_std)
 
 
 if __name__ == "__main__":

@@ -6,6 +6,9 @@
   20-iteration extended/cubature smoothers (notebooks/robustness_100runs.py).
   The reference's values are FP32, so a run may settle on another fixed point
   in FP32 than in FP64; the test requires most runs to agree to 1e-5 (extended).
+  The covariance-form values of the same study pin the oracle's covariance form,
+  and record the study's finding: FP32 covariance-form cubature fails (NaN)
+  where the square-root form does not.
 """
 import os
 
@@ -71,3 +74,42 @@ def test_robustness_loglikelihood_cubature_t50():
         g = float(d["ell_cubature"][ti, run])
         rel.append(abs(ell - g) / abs(g))
     assert np.mean(np.array(rel) < 1e-2) >= 0.8, rel
+
+
+def _robustness_ell_standard(lin, T, run, ys):
+    """The covariance-form run of the same study (notebooks/robustness_100runs.py, std models)."""
+    from oracle.types import MVNStandard
+    Q, R = OM.bearings_noise(0.01, 0.1, 0.5, 0.01)
+    tm = FunctionalModel(OM.CoordinatedTurn(0.01), MVNStandard(np.zeros(5), Q))
+    om = FunctionalModel(OM.Bearings([-1.5, 0.5], [1.0, 1.0]), MVNStandard(np.zeros(2), R))
+    x0 = MVNStandard(np.array([-4.0, -1.0, 2.0, 7.0, 3.0]), np.eye(5))
+    nom = MVNStandard(np.repeat(np.array([[-1.0, -1.0, 6.0, 4.0, 2.0]]), T + 1, 0),
+                      np.repeat(np.eye(5)[None], T + 1, 0))
+    _, ell = M.iterated_smoothing(ys[run, :T].astype(float), x0, tm, om, lin, nom, True,
+                                  criterion=lambda i, *_: i < 20, return_loglikelihood=True)
+    return ell
+
+
+@pytest.mark.parametrize("T", [20, 50, 100])
+def test_robustness_loglikelihood_extended_standard(T):
+    # the reference's FP32 covariance-form extended smoother: the oracle's covariance form
+    # (FP64) agrees to 1e-5 on most runs, as the square-root form does
+    d = np.load(os.path.join(GOLD, "robustness_small.npz"))
+    ti = list(d["Ts"]).index(T)
+    rel = []
+    for run in range(d["ys"].shape[0]):
+        g = float(d["ell_extended_std"][ti, run])
+        rel.append(abs(_robustness_ell_standard(LZ.extended, T, run, d["ys"]) - g) / abs(g))
+    assert np.mean(np.array(rel) < 1e-5) >= 0.8, rel
+
+
+def test_robustness_covariance_form_cubature_fails_in_fp32_only():
+    # the reference's robustness finding at T = 100: its FP32 covariance-form cubature smoother
+    # returns NaN on every run while its FP32 square-root form is finite; in FP64 the
+    # covariance form is finite too, so the failure is the FP32 arithmetic of that form
+    d = np.load(os.path.join(GOLD, "robustness_small.npz"))
+    ti = list(d["Ts"]).index(100)
+    assert np.isnan(d["ell_cubature_std"][ti]).all()
+    assert np.isfinite(d["ell_cubature"][ti]).all()
+    for run in range(0, d["ys"].shape[0], 4):
+        assert np.isfinite(_robustness_ell_standard(LZ.cubature, 100, run, d["ys"]))
