@@ -20,5 +20,5 @@ from .types import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsMode
 from . import models, linearization, parallel, sequential, methods
 
 __all__ = ["tria", "canon", "cholesky_update", "cholesky_update_many", "mvn_loglikelihood",
-           "solve_lower", "solve_upper", "MVNSqrt", "MVNStandard", "FunctionalModel",
+           "solve_lower", "solve_upper", "MVNSqrt", "MVNStandard", "FunctionalModel", "ConditionalMomentsModel",
            "models", "linearization", "parallel", "sequential", "methods"]

@@ -9,7 +9,7 @@ second, association-independent truth.
 import numpy as np
 
 from .core import tria, mT, mv, mvn_loglikelihood
-from .types import MVNSqrt, MVNStandard, are_inputs_compatible
+from .types import MVNSqrt, are_inputs_compatible
 
 
 # ----------------------------------------------------------------------------- scans

@@ -6,8 +6,8 @@ path's association-independent counterpart.
 """
 import numpy as np
 
-from .core import tria, mT, mv, mvn_loglikelihood
-from .types import MVNSqrt, MVNStandard, are_inputs_compatible
+from .core import tria, mv, mvn_loglikelihood
+from .types import MVNSqrt, are_inputs_compatible
 
 
 def _lin_one(method, model, x):

@@ -11,7 +11,6 @@ import torch
 
 import oracle as O
 import sqrt_parallel_smoothers_gb300 as S
-from sqrt_parallel_smoothers_gb300 import models as GM
 from tests._parity import linear_pair, np_
 
 pytestmark = pytest.mark.gpu
