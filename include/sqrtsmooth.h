@@ -165,7 +165,10 @@ int ss_iterated(const ss_problem* p, const void* ys, const void* m0, const void*
  * process exits.  Problems whose ss_workspace_bytes exceed it are rejected
  * with SS_ERR_WORKSPACE.  The first call on a device looks up the array's
  * device address (cudaGetSymbolAddress, with that device current); make that
- * first call before any stream capture.  All calls share the one array, so
+ * first call before any stream capture.  The address is remembered per device
+ * for the life of the process: it does not survive cudaDeviceReset or any
+ * other teardown of the device's primary context, after which this entry
+ * point must not be called again in the same process.  All calls share the one array, so
  * calls whose GPU work overlaps (other streams, other threads) race and must
  * be serialised by the caller; a call fully rewrites what it reads, so no
  * clearing between calls is needed.  Allocates nothing. */

@@ -59,6 +59,31 @@ SS_DEV void reflector(float x0, float sigma, float& beta, float& v0, float& k) {
   }
 }
 
+// Range guard of the FP32 reflectors.  A reflector takes the unscaled sum of
+// squares of its row, which overflows once an entry passes about 1.8e19 (and
+// the products of its update a little earlier), and underflows below about
+// 1e-19.  When x0^2 + sigma leaves [2^-64, 2^64] (or is not finite) the row is
+// scaled by a power of two first, as LAPACK's scaled norm does: every step of
+// the reflector is then exact in range, and the reflector itself is unchanged
+// (H = I + k u u^T is invariant under u -> a u, k -> k / a^2), so only beta is
+// scaled back.  Typical rows never take this path; FP64 (range 1e308) and dual
+// numbers never do.
+template <typename R>
+SS_DEV bool reflector_out_of_range(const R&, const R&) { return false; }
+SS_DEV bool reflector_out_of_range(float x0, float sigma) {
+  const float s = x0 * x0 + sigma;
+  return !(s <= 0x1p64f && s >= 0x1p-64f);
+}
+// 2^-e for the exponent e of amax (amax > 0), so that amax * 2^-e lies in
+// [1, 2); e is clamped so that both 2^-e and 2^e are normal floats.
+SS_DEV float pow2_inverse_scale(float amax) {
+  int e = ((__float_as_int(amax) >> 23) & 0xff) - 127;
+  e = e < -125 ? -125 : (e > 125 ? 125 : e);
+  return __int_as_float((127 - e) << 23);
+}
+template <typename R>
+SS_DEV R pow2_inverse_scale(const R&) { return R(1); }
+
 // Programmatic dependent launch (sm_90 and later).  The per-pass kernels are
 // launched with programmatic stream serialisation, so a kernel's launch is
 // prepared while its predecessor on the stream drains.  Each such kernel calls
@@ -95,10 +120,25 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
       if ((j - i) & 1) sig0 += M[i][j] * M[i][j];
       else sig1 += M[i][j] * M[i][j];
     }
-    const R sigma = sig0 + sig1;
-    const R x0 = M[i][i];
+    R sigma = sig0 + sig1;
+    R x0 = M[i][i];
     R beta = x0;
     if (sigma != R(0)) {
+      R unscale = R(1);
+      if (reflector_out_of_range(x0, sigma)) {
+        R amax = ss_abs(x0);
+        SS_UNROLL
+        for (int j = i + 1; j < COLS; ++j) amax = ss_abs(M[i][j]) > amax ? ss_abs(M[i][j]) : amax;
+        const R sc = pow2_inverse_scale(amax);
+        unscale = R(1) / sc;
+        x0 *= sc;
+        sigma = R(0);
+        SS_UNROLL
+        for (int j = i + 1; j < COLS; ++j) {
+          M[i][j] *= sc;
+          sigma += M[i][j] * M[i][j];
+        }
+      }
       const R nrm = ss_sqrt(x0 * x0 + sigma);
       beta = (x0 <= R(0)) ? nrm : -nrm;   // opposite sign of x0: no cancellation in v0
       const R v0 = x0 - beta;
@@ -122,6 +162,7 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
       }
       SS_UNROLL
       for (int j = i + 1; j < COLS; ++j) M[i][j] = R(0);
+      beta *= unscale;
     }
     // canonical sign: non-negative diagonal (flip column i)
     if (beta < R(0)) {
@@ -216,13 +257,32 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
           else sig1 += M[i][j] * M[i][j];
         }
       }
-      const R sigma = sig0 + sig1;
-      const R x0 = M[i][i];
+      R sigma = sig0 + sig1;
+      R x0 = M[i][i];
       if (sigma != R(0)) {
         // H = I + u u^T / (beta v0), u = (v0, M[i][i+1:]), v0 = x0 - beta:
-        // one reciprocal per reflector, no scaled copy of the row.
-        R v0, k;
+        // one reciprocal per reflector, no scaled copy of the row (except in
+        // the FP32 range guard, which scales the row in place).
+        R v0, k, unscale = R(1);
+        if (reflector_out_of_range(x0, sigma)) {
+          R amax = ss_abs(x0);
+          SS_UNROLL
+          for (int j = i + 1; j < COLS; ++j)
+            if ((SUP >> j) & 1) amax = ss_abs(M[i][j]) > amax ? ss_abs(M[i][j]) : amax;
+          const R sc = pow2_inverse_scale(amax);
+          unscale = R(1) / sc;
+          x0 *= sc;
+          sigma = R(0);
+          SS_UNROLL
+          for (int j = i + 1; j < COLS; ++j) {
+            if ((SUP >> j) & 1) {
+              M[i][j] *= sc;
+              sigma += M[i][j] * M[i][j];
+            }
+          }
+        }
         reflector(x0, sigma, beta, v0, k);
+        beta *= unscale;
         SS_UNROLL
         for (int r = i + 1; r < ROWS; ++r) {
           if ((TOUCH >> r) & 1) {
@@ -326,7 +386,12 @@ SS_DEV void chol_add_column(R (&L)[D][D], R (&v)[D]) {
   for (int j = 0; j < D; ++j) {
     const R a = L[j][j];
     const R b = v[j];
-    const R r = ss_sqrt(a * a + b * b);
+    R r = ss_sqrt(a * a + b * b);
+    if (r != R(0) && reflector_out_of_range(a, b * b)) {   // FP32 range guard, as in the reflectors
+      const R amax = ss_abs(a) > ss_abs(b) ? ss_abs(a) : ss_abs(b);
+      const R sc = pow2_inverse_scale(amax);
+      r = ss_sqrt((a * sc) * (a * sc) + (b * sc) * (b * sc)) / sc;
+    }
     if (r != R(0)) {
       const R c = a / r, s = b / r;
       L[j][j] = r;

@@ -1,12 +1,12 @@
 """Copy the reference's golden vectors for the smoother path into ``tests/golden/``.
 
-Run once in a checkout that has the reference mounted (read-only) at
-``/root/reference``; the outputs are committed so the tests never read the
-reference at run time.
+Run once with the path of a checkout of the reference as the argument
+(``python make_golden.py <reference checkout>``); the outputs are committed so
+the tests never read the reference at run time.
 
-* ``bearings_ys.npy``, ``ieks.npz`` - observations and 100-iteration extended
-  smoother output of the bearings regression test
-  (tests/test_bearings_only.py:25-72 of the reference).
+* ``bearings_ys.npy``, ``ieks.npz``, ``icks.npz`` - observations and the
+  100-iteration extended and cubature smoother outputs of the bearings
+  regression test (tests/test_bearings_only.py:25-72 of the reference).
 * ``robustness_small.npz`` - the first 100 observations of runs 1..20 of
   ``notebooks/robustness_data/data-T8000-Run*.npz`` and the FP32 GPU
   log-likelihoods the reference computed on them for T in 20..100
@@ -16,17 +16,19 @@ reference at run time.
 """
 import os
 import shutil
+import sys
 
 import numpy as np
 
-REF = "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main():
+def main(REF):
     shutil.copyfile(f"{REF}/tests/bearings/ys.npy", f"{HERE}/bearings_ys.npy")
     with np.load(f"{REF}/tests/bearings/ieks.npz") as d:
         np.savez_compressed(f"{HERE}/ieks.npz", mean=d["arr_0"], cov=d["arr_1"])
+    with np.load(f"{REF}/tests/bearings/icks.npz") as d:
+        np.savez_compressed(f"{HERE}/icks.npz", mean=d["arr_0"], cov=d["arr_1"])
     base = f"{REF}/notebooks/robustness_data"
     runs = 20
     ys = np.stack([np.load(f"{base}/data-T8000-Run{j + 1}.npz")["data"][:100] for j in range(runs)])
@@ -44,4 +46,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference checkout>")
+    main(sys.argv[1])
