@@ -67,7 +67,12 @@ SS_DEV void reflector(float x0, float sigma, float& beta, float& v0, float& k) {
 // the reflector is then exact in range, and the reflector itself is unchanged
 // (H = I + k u u^T is invariant under u -> a u, k -> k / a^2), so only beta is
 // scaled back.  Typical rows never take this path; FP64 (range 1e308) and dual
-// numbers never do.
+// numbers never do.  The guard is not free even when no row takes it (with it
+// on every tria the batched smoother measured 16 % slower, the filter walk
+// 28 %), so tria and tria_sp take it as a template flag, set where FP32 entries
+// can grow without bound: the information-factor update of the chunk leaf,
+// whose rows carry the chunk's product of linearised transitions
+// (filter_extend, csrc/ss_ops.cuh; 1.5 % of the batched smoother's time).
 template <typename R>
 SS_DEV bool reflector_out_of_range(const R&, const R&) { return false; }
 SS_DEV bool reflector_out_of_range(float x0, float sigma) {
@@ -108,7 +113,7 @@ SS_DEV void pdl_enter() {
 // applied from the right, one per row (the transpose of QR of M^T).  This is
 // the single primitive every square-root step uses
 // (parsmooth/_utils.py:22-24 computes the same factor through jnp.linalg.qr).
-template <typename R, int ROWS, int COLS>
+template <typename R, int ROWS, int COLS, bool GUARD = false>
 SS_DEV void tria(R (&M)[ROWS][COLS]) {
   static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
   SS_UNROLL
@@ -125,7 +130,7 @@ SS_DEV void tria(R (&M)[ROWS][COLS]) {
     R beta = x0;
     if (sigma != R(0)) {
       R unscale = R(1);
-      if (reflector_out_of_range(x0, sigma)) {
+      if (GUARD && reflector_out_of_range(x0, sigma)) {
         R amax = ss_abs(x0);
         SS_UNROLL
         for (int j = i + 1; j < COLS; ++j) amax = ss_abs(M[i][j]) > amax ? ss_abs(M[i][j]) : amax;
@@ -240,7 +245,7 @@ struct PatFull {
   __host__ __device__ static constexpr bool nz(int, int) { return true; }
 };
 
-template <typename R, int ROWS, int COLS, class PAT, int I>
+template <typename R, int ROWS, int COLS, class PAT, int I, bool GUARD>
 SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
   if constexpr (I < ROWS) {
     constexpr TriaPlan<ROWS, COLS> P = make_tria_plan<ROWS, COLS, PAT>();
@@ -264,7 +269,7 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
         // one reciprocal per reflector, no scaled copy of the row (except in
         // the FP32 range guard, which scales the row in place).
         R v0, k, unscale = R(1);
-        if (reflector_out_of_range(x0, sigma)) {
+        if (GUARD && reflector_out_of_range(x0, sigma)) {
           R amax = ss_abs(x0);
           SS_UNROLL
           for (int j = i + 1; j < COLS; ++j)
@@ -312,11 +317,11 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
     } else {
       M[i][i] = beta;
     }
-    tria_sp_step<R, ROWS, COLS, PAT, I + 1>(M);
+    tria_sp_step<R, ROWS, COLS, PAT, I + 1, GUARD>(M);
   }
 }
 
-template <typename R, int ROWS, int COLS, class PAT>
+template <typename R, int ROWS, int COLS, class PAT, bool GUARD = false>
 SS_DEV void tria_sp(R (&M)[ROWS][COLS]) {
   static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
   // entries outside the pattern are zero: say so, so that they cost no registers
@@ -326,7 +331,7 @@ SS_DEV void tria_sp(R (&M)[ROWS][COLS]) {
     for (int c = 0; c < COLS; ++c)
       if (!PAT::nz(r, c)) M[r][c] = R(0);
   }
-  tria_sp_step<R, ROWS, COLS, PAT, 0>(M);
+  tria_sp_step<R, ROWS, COLS, PAT, 0, GUARD>(M);
 }
 
 // ---------------------------------------------------------------------------
@@ -386,12 +391,7 @@ SS_DEV void chol_add_column(R (&L)[D][D], R (&v)[D]) {
   for (int j = 0; j < D; ++j) {
     const R a = L[j][j];
     const R b = v[j];
-    R r = ss_sqrt(a * a + b * b);
-    if (r != R(0) && reflector_out_of_range(a, b * b)) {   // FP32 range guard, as in the reflectors
-      const R amax = ss_abs(a) > ss_abs(b) ? ss_abs(a) : ss_abs(b);
-      const R sc = pow2_inverse_scale(amax);
-      r = ss_sqrt((a * sc) * (a * sc) + (b * sc) * (b * sc)) / sc;
-    }
+    const R r = ss_sqrt(a * a + b * b);
     if (r != R(0)) {
       const R c = a / r, s = b / r;
       L[j][j] = r;

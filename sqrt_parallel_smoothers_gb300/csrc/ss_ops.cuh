@@ -421,7 +421,10 @@ SS_DEV void filter_extend(FElem<R, NX>& a, const Lin<R, NX, NY>& l, const R (&y)
     SS_UNROLL
     for (int k = 0; k < NY; ++k) Zx[i][NX + k] = W[k][i];
   }
-  tria_sp<R, NX, NX + NY, ZExtPat<NX, AZK>>(Zx);
+  // The one FP32 range-guarded tria of the pass (ss_la.cuh): W carries the chunk's product
+  // of linearised transitions (Ap = F A), which a divergent Gauss-Newton iterate can grow
+  // past FP32's range for squares; the other trias of the pass see bounded entries.
+  tria_sp<R, NX, NX + NY, ZExtPat<NX, AZK>, true>(Zx);
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
