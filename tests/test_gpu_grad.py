@@ -155,3 +155,25 @@ def test_bearings_theta_gradient_through_iterations(dtype, tol):
                                               S.MVNSqrt(torch.as_tensor(nom_m), torch.as_tensor(nom_L)), Q1, 0.01,
                                               (1.0, 1.0), S.linearization.cubature, None, None)
     assert abs(float(dirs_only.detach()) - float(ell.detach())) > 1e-6 * abs(float(ell.detach()))
+
+
+def test_iterated_gradient_equals_implicit_derivative_at_fixed_point():
+    """At a converged bearings fixed point (20 calls, FP64) the derivative of the unrolled
+    iteration (ss_iterated_grad) equals the reference's implicit-function derivative
+    (parsmooth/_utils.py:108-133: the truncated Neumann series of n_iter + 1 adjoint sweeps),
+    restated in oracle/implicit.py."""
+    from oracle import implicit
+    from tests.test_oracle_implicit import bearings_theta_models, converged_problem, iterated_ell
+    ys, m0, nom, Q1, theta0, n_iter = converged_problem()
+    x_star, _ = iterated_ell(theta0, ys, m0, nom, Q1, n_iter, with_traj=True)
+    ref, _ = implicit.iterated_loglikelihood_grad(lambda th: bearings_theta_models(th, Q1), theta0, ys,
+                                                 O.MVNSqrt(m0, np.eye(5)), O.linearization.cubature, x_star, n_iter)
+    theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
+    ell = S.BearingsLogLikelihood.apply(theta, torch.as_tensor(ys),
+                                        S.MVNSqrt(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64)),
+                                        S.MVNSqrt(torch.as_tensor(nom.mean), torch.as_tensor(nom.chol)), Q1, 0.01,
+                                        (1.0, 1.0), S.linearization.cubature, None, None, n_iter)
+    ell.backward()
+    g = theta.grad.numpy()
+    rel = np.abs(g - ref) / np.maximum(np.abs(ref), 1.0)
+    assert np.all(rel <= 1e-6), (g, ref, rel)
