@@ -82,6 +82,16 @@ typedef struct ss_model {
  * computes every factor once and only the means per sequence (up to 32 sequences).  This
  * bit forces the per-sequence computation instead. */
 #define SS_OPT_PER_SEQUENCE_COVARIANCE 1
+/* Covariance form: every factor argument of ss_linearize, ss_filter, ss_smooth and
+ * ss_iterated is a covariance instead of a lower Cholesky factor (the models'
+ * noise_chol, L0, the nominal, filtered and output trajectories, and the linearised
+ * noise of ss_linearize), and the calls run the reference's covariance-form
+ * ("standard") elements, operators and linearisation: parsmooth/parallel/_operators.py:7-40
+ * and 80-101, parsmooth/parallel/_filtering.py:64-97 and 157-163,
+ * parsmooth/parallel/_smoothing.py:60-69, parsmooth/linearization/_sigma_points.py:39-60
+ * and 81-86, in the problem's precision.  Built for nx <= 5, ny <= 3 (not the
+ * large-state pairs); the workspace query must see the bit. */
+#define SS_OPT_COVARIANCE_FORM 2
 
 typedef struct ss_problem {
   int32_t dtype;           /* SS_F32 or SS_F64 */

@@ -16,6 +16,7 @@ SS_MODEL_LINEAR, SS_MODEL_COORDINATED_TURN, SS_MODEL_BEARINGS, SS_MODEL_RICKER, 
 SS_MAX_GH_ORDER = 8
 SS_MAX_TANGENTS = 4
 SS_OPT_PER_SEQUENCE_COVARIANCE = 1
+SS_OPT_COVARIANCE_FORM = 2
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
             "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",

@@ -181,6 +181,8 @@ static int validate(const ss_problem* p) {
     if (m->kind < SS_MODEL_LINEAR || m->kind > SS_MODEL_POISSON_EXP) return SS_ERR_UNSUPPORTED;
   }
   if (find_run(p->dtype, p->nx, p->ny) == nullptr) return SS_ERR_UNSUPPORTED;
+  // the covariance-form kernels exist for the small-state pairs only
+  if ((p->options & SS_OPT_COVARIANCE_FORM) && (p->nx > SS_MAX_NX || p->ny > SS_MAX_NY)) return SS_ERR_UNSUPPORTED;
   return SS_OK;
 }
 

@@ -602,11 +602,21 @@ struct Runner {
   }
 };
 
+// Covariance-form calls (ss_problem.options & SS_OPT_COVARIANCE_FORM): defined in
+// ss_std_run.cuh and instantiated in their own translation units (inst_std_*.cu),
+// which keeps the parallel build's longest unit short.
+template <typename R, int NX, int NY>
+int run_std(const Call& c);
+
 template <typename R, int NX, int NY>
 int run(const Call& c) {
   if (c.op == OP_SUPPORTED)
     return models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind) ? SS_OK : SS_ERR_UNSUPPORTED;
   if (!models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind)) return SS_ERR_UNSUPPORTED;
+  if (c.p->options & SS_OPT_COVARIANCE_FORM) {
+    if constexpr (Tangents<R>::n == 0) return run_std<R, NX, NY>(c);
+    else return SS_ERR_UNSUPPORTED;
+  }
   if (c.op == OP_WORKSPACE) {
     Layout y;
     const int rc = make_layout<R, NX, NY>(*c.p, y);

@@ -210,11 +210,16 @@ def _model_tensors(model, d_in, d_out, dtype, device, sqrt=True):
     return fn, mat, qm, qL
 
 
-def _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, extra):
+# Bit of the slr_form slot of the integer config that selects the covariance-form kernels
+# (ss_problem.options SS_OPT_COVARIANCE_FORM); the slot's low bits keep the SLR form.
+_COV_FLAG = 16
+
+
+def _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, slr_form, extra, cov=False):
     p = method.params
     kappa_default = 1 if p.get("kappa", None) is None else 0
-    return [nx, ny, method.code, kappa_default, int(p.get("order", 3)), int(slr_form), int(chunk), int(group),
-            fn_t.kind, fn_o.kind, lay.B, lay.N, lay.max_len] + list(extra)
+    return [nx, ny, method.code, kappa_default, int(p.get("order", 3)), int(slr_form) | (_COV_FLAG if cov else 0),
+            int(chunk), int(group), fn_t.kind, fn_o.kind, lay.B, lay.N, lay.max_len] + list(extra)
 
 
 def _fcfg(method, fn_t, fn_o, extra=()):
@@ -259,10 +264,12 @@ def _problem(icfg, fcfg, dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL):
     (nx, ny, code, kdef, order, slr, chunk, group, tk, ok, B, N, maxlen) = icfg[:13]
     pr = _lib.SSProblem()
     pr.options = _lib.SS_OPT_PER_SEQUENCE_COVARIANCE if _OPTIONS["per_sequence_covariance"] else 0
+    if slr & _COV_FLAG:
+        pr.options |= _lib.SS_OPT_COVARIANCE_FORM
     pr.dtype = _DT[dtype]
     pr.nx, pr.ny, pr.lin_method = nx, ny, code
     pr.ut_alpha, pr.ut_beta, pr.ut_kappa = fcfg[0], fcfg[1], fcfg[2]
-    pr.ut_kappa_default, pr.gh_order, pr.slr_form = kdef, order, slr
+    pr.ut_kappa_default, pr.gh_order, pr.slr_form = kdef, order, slr & ~_COV_FLAG
     pr.chunk, pr.group = chunk, group
     for mdl, kind, mat, qm, qL, par in ((pr.transition, tk, t_mat, t_qm, t_qL, fcfg[3:7]),
                                         (pr.observation, ok, o_mat, o_qm, o_qL, fcfg[7:11])):
@@ -492,6 +499,57 @@ def _model_to_sqrt(model):
     return model
 
 
+# Covariance-form ("standard") inputs: by default they run the reference's covariance-form
+# operators on the GPU (csrc/ss_std.cuh); covariance_form="factored" factors them instead and runs
+# the square-root kernels (results returned as covariances).
+_COV_FORMS = ("operators", "factored")
+
+
+def _cov_form(covariance_form):
+    if covariance_form not in _COV_FORMS:
+        raise ValueError(f"covariance_form must be one of {_COV_FORMS}, got {covariance_form!r}")
+    return covariance_form == "operators"
+
+
+def _model_tensors_std(model, d_in, d_out, dtype, device):
+    """Device model with its noise mean and covariance (covariance-form kernels)."""
+    if isinstance(model, ConditionalMomentsModel):
+        return _model_tensors(model, d_in, d_out, dtype, device)   # the model gives its conditional covariances
+    if not isinstance(model, FunctionalModel):
+        raise TypeError(f"expected a FunctionalModel, got {type(model).__name__}")
+    fn = as_device_model(model.function)
+    if fn.d_out != d_out or fn.d_in != d_in:
+        raise ValueError(f"{fn!r} maps R^{fn.d_in} -> R^{fn.d_out}, expected R^{d_in} -> R^{d_out}")
+    q = model.mvn
+    if not isinstance(q, MVNStandard):
+        raise TypeError(f"All inputs should have the same type: an MVNSqrt noise with MVNStandard states ({model!r})")
+    qm = _as(q.mean, dtype, device).reshape(d_out)
+    Q = _as(q.cov, dtype, device).reshape(d_out, d_out).contiguous()
+    mat = fn.matrix()
+    mat = None if mat is None else _as(mat, dtype, device)
+    return fn, mat, qm, Q
+
+
+def _prior_std(x0, lay, nx):
+    m0 = _as(x0.mean, lay.dtype, lay.device)
+    P0 = _as(x0.cov, lay.dtype, lay.device)
+    if m0.ndim == 1:
+        return m0.reshape(1, nx), P0.reshape(1, nx, nx).contiguous(), 0
+    if m0.shape[0] != lay.B:
+        raise ValueError("a per-sequence prior needs one mean per sequence")
+    P0 = P0.expand(lay.B, nx, nx) if P0.ndim == 2 else P0
+    return m0.contiguous(), P0.contiguous(), 1
+
+
+def _nominal_std(nominal, lay, nx):
+    if nominal is None:
+        return None, None
+    if not isinstance(nominal, MVNStandard):
+        raise TypeError("All inputs should have the same type: an MVNSqrt nominal trajectory with an "
+                        "MVNStandard prior")
+    return lay.pack_states(nominal.mean, (nx,)), lay.pack_states(nominal.cov, (nx, nx)).contiguous()
+
+
 def _check_common(x0, parallel, method):
     if not parallel:
         raise NotImplementedError("only parallel=True is implemented on the GPU")
@@ -535,15 +593,20 @@ def _dummy_ny(nx):
 
 def filtering(observations, x0, transition_model, observation_model, linearization_method,
               nominal_trajectory=None, parallel=True, return_loglikelihood=False, *, lengths=None,
-              offsets=None, chunk=0, group=0, slr_form=0):
+              offsets=None, chunk=0, group=0, slr_form=0, covariance_form="operators"):
     """Parallel square-root filter (parsmooth/methods.py:14-26 -> parsmooth/parallel/_filtering.py:13-61).
 
-    Covariance-form inputs (``MVNStandard`` prior, nominal and model noises, the reference's
-    standard filter) are factored by torch where the tensors live (the GPU for CUDA inputs),
-    filtered by the square-root kernels and returned as covariances."""
+    Covariance-form inputs (``MVNStandard`` prior, nominal and model noises) run the reference's
+    standard filter: its covariance-form linearisation, elements and combine
+    (parsmooth/parallel/_filtering.py:64-97, parsmooth/parallel/_operators.py:7-40) in CUDA
+    kernels.  ``covariance_form="factored"`` instead factors the covariances (torch, where the
+    tensors live), runs the square-root kernels and returns covariances."""
     if isinstance(x0, MVNStandard):
         if nominal_trajectory is not None:
             are_inputs_compatible(x0, nominal_trajectory)
+        if _cov_form(covariance_form):
+            return _filtering_std(observations, x0, transition_model, observation_model, linearization_method,
+                                  nominal_trajectory, parallel, return_loglikelihood, lengths, offsets, chunk, group)
         out = filtering(observations, _std_to_sqrt(x0), _model_to_sqrt(transition_model),
                         _model_to_sqrt(observation_model), linearization_method, _std_to_sqrt(nominal_trajectory),
                         parallel, return_loglikelihood, lengths=lengths, offsets=offsets, chunk=chunk, group=group,
@@ -571,15 +634,79 @@ def filtering(observations, x0, transition_model, observation_model, linearizati
     return res
 
 
+def _filtering_std(observations, x0, transition_model, observation_model, linearization_method, nominal_trajectory,
+                   parallel, return_loglikelihood, lengths, offsets, chunk, group):
+    """The covariance-form filter on the GPU (ss_filter with SS_OPT_COVARIANCE_FORM)."""
+    if not parallel:
+        raise NotImplementedError("only parallel=True is implemented on the GPU")
+    method = resolve(linearization_method)
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_Q = _model_tensors_std(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_Q = _model_tensors_std(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, P0, per = _prior_std(x0, lay, nx)
+    nm, nP = _nominal_std(nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, 0, [per, int(bool(return_loglikelihood))],
+                 cov=True)
+    out_m, out_P, ell = torch.ops.sqrtsmooth.filter(lay.ys, lay.offsets, m0, P0, nm, nP, t_mat, t_qm, t_Q,
+                                                    o_mat, o_qm, o_Q, icfg, _fcfg(method, fn_t, fn_o))
+    res = MVNStandard(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_P, (nx, nx)))
+    if return_loglikelihood:
+        return res, lay.per_sequence(ell)
+    return res
+
+
+def _smooth_layout(fm, lengths, offsets, dtype, dev):
+    """Batch geometry from a trajectory's shape (T+1 states per sequence)."""
+    if offsets is not None:
+        off = torch.as_tensor(offsets, dtype=torch.int64)
+        return _Layout(torch.zeros((int(off[-1]), 1), dtype=dtype), None, off, dtype, dev)
+    if fm.ndim == 2:
+        return _Layout(torch.zeros((fm.shape[0] - 1, 1), dtype=dtype), None, None, dtype, dev)
+    B, Tp1 = fm.shape[:2]
+    return _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
+
+
+def _smoothing_std(transition_model, filter_trajectory, linearization_method, nominal_trajectory, parallel,
+                   lengths, offsets, chunk, group):
+    """The covariance-form smoother on the GPU (ss_smooth with SS_OPT_COVARIANCE_FORM)."""
+    if not parallel:
+        raise NotImplementedError("only parallel=True is implemented on the GPU")
+    method = resolve(linearization_method)
+    dev = _device()
+    fm = filter_trajectory.mean if isinstance(filter_trajectory.mean, torch.Tensor) else \
+        torch.as_tensor(filter_trajectory.mean)
+    nx = int(fm.shape[-1])
+    dtype = fm.dtype if fm.dtype in _DT else torch.float32
+    lay = _smooth_layout(fm, lengths, offsets, dtype, dev)
+    fn_t, t_mat, t_qm, t_Q = _model_tensors_std(transition_model, nx, nx, lay.dtype, dev)
+    ny = _dummy_ny(nx)
+    fn_o, o_mat, o_qm, o_Q = _dummy_observation(nx, lay.dtype, dev, ny)
+    fmp = lay.pack_states(filter_trajectory.mean, (nx,))
+    fPp = lay.pack_states(filter_trajectory.cov, (nx, nx)).contiguous()
+    nm, nP = _nominal_std(nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, ny, fn_t, fn_o, lay, chunk, group, 0, [0, 0], cov=True)
+    out_m, out_P = torch.ops.sqrtsmooth.smooth(fmp, fPp, lay.offsets, nm, nP, t_mat, t_qm, t_Q, o_mat, o_qm,
+                                               o_Q, icfg, _fcfg(method, fn_t, fn_o))
+    return MVNStandard(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_P, (nx, nx)))
+
+
 def smoothing(transition_model, filter_trajectory, linearization_method, nominal_trajectory=None,
-              parallel=True, *, lengths=None, offsets=None, chunk=0, group=0, slr_form=0):
+              parallel=True, *, lengths=None, offsets=None, chunk=0, group=0, slr_form=0,
+              covariance_form="operators"):
     """Parallel square-root RTS smoother (parsmooth/methods.py:29-35 -> parsmooth/parallel/_smoothing.py:14-44).
 
     For batches pass ``lengths`` (padded trajectories ``(B, T+1, ...)``) or
-    ``offsets`` (packed trajectories, offsets of the steps)."""
+    ``offsets`` (packed trajectories, offsets of the steps).  A covariance-form filtered
+    trajectory runs the reference's standard smoother (parsmooth/parallel/_smoothing.py:60-69,
+    parsmooth/parallel/_operators.py:80-101) unless ``covariance_form="factored"``."""
     if isinstance(filter_trajectory, MVNStandard):
         if nominal_trajectory is not None:
             are_inputs_compatible(filter_trajectory, nominal_trajectory)
+        if _cov_form(covariance_form):
+            return _smoothing_std(transition_model, filter_trajectory, linearization_method, nominal_trajectory,
+                                  parallel, lengths, offsets, chunk, group)
         return _sqrt_to_std(smoothing(_model_to_sqrt(transition_model), _std_to_sqrt(filter_trajectory),
                                       linearization_method, _std_to_sqrt(nominal_trajectory), parallel,
                                       lengths=lengths, offsets=offsets, chunk=chunk, group=group,
@@ -684,14 +811,15 @@ def filter_smoother(observations, x0, transition_model, observation_model, linea
     """parsmooth/methods.py:38-47."""
     filt = filtering(observations, x0, transition_model, observation_model, linearization_method,
                      nominal_trajectory, parallel, **kw)
-    kw = {k: v for k, v in kw.items() if k in ("lengths", "offsets", "chunk", "group", "slr_form")}
+    kw = {k: v for k, v in kw.items() if k in ("lengths", "offsets", "chunk", "group", "slr_form",
+                                               "covariance_form")}
     return smoothing(transition_model, filt, linearization_method, nominal_trajectory, parallel, **kw)
 
 
 def iterated_smoothing(observations, x0, transition_model, observation_model, linearization_method,
                        init_nominal_trajectory=None, parallel=True, criterion=_default_criterion,
                        return_loglikelihood=False, *, lengths=None, offsets=None, chunk=0, group=0,
-                       slr_form=0, return_info=False):
+                       slr_form=0, return_info=False, covariance_form="operators"):
     """Iterated square-root smoother (parsmooth/methods.py:54-76), the whole loop on the device.
 
     ``criterion`` may be a count test such as ``lambda i, *_: i < N`` (exactly
@@ -699,11 +827,16 @@ def iterated_smoothing(observations, x0, transition_model, observation_model, li
     :class:`MeanSquaredChange` / :class:`FixedIterations`.  With
     ``return_info=True`` a dict with per-sequence ``iterations`` and status
     ``flags`` (1 non-finite output, 2 non-finite log-likelihood, 4 not
-    converged) is returned last.  Covariance-form inputs are factored and the result returned
-    as covariances (see :func:`filtering`)."""
+    converged) is returned last.  Covariance-form inputs run the reference's covariance-form
+    filter and smoother in every call, or (``covariance_form="factored"``) are factored and the
+    result returned as covariances (see :func:`filtering`)."""
     if isinstance(x0, MVNStandard):
         if init_nominal_trajectory is not None:
             are_inputs_compatible(x0, init_nominal_trajectory)
+        if _cov_form(covariance_form):
+            return _iterated_std(observations, x0, transition_model, observation_model, linearization_method,
+                                 init_nominal_trajectory, parallel, criterion, return_loglikelihood, lengths,
+                                 offsets, chunk, group, return_info)
         out = iterated_smoothing(observations, _std_to_sqrt(x0), _model_to_sqrt(transition_model),
                                  _model_to_sqrt(observation_model), linearization_method,
                                  _std_to_sqrt(init_nominal_trajectory), parallel, criterion, return_loglikelihood,
@@ -737,14 +870,46 @@ def iterated_smoothing(observations, x0, transition_model, observation_model, li
     return out[0] if len(out) == 1 else out
 
 
-def linearize(model, x, method):
+def _iterated_std(observations, x0, transition_model, observation_model, linearization_method,
+                  init_nominal_trajectory, parallel, criterion, return_loglikelihood, lengths, offsets, chunk,
+                  group, return_info):
+    """The covariance-form iterated smoother on the GPU (ss_iterated with SS_OPT_COVARIANCE_FORM)."""
+    if not parallel:
+        raise NotImplementedError("only parallel=True is implemented on the GPU")
+    method = resolve(linearization_method)
+    n_calls, tol = _criterion_schedule(criterion)
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_Q = _model_tensors_std(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_Q = _model_tensors_std(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, P0, per = _prior_std(x0, lay, nx)
+    im, iP = _nominal_std(init_nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, 0,
+                 [per, int(bool(return_loglikelihood)), n_calls], cov=True)
+    fcfg = _fcfg(method, fn_t, fn_o, [tol])
+    out_m, out_P, ell, iters, flags = torch.ops.sqrtsmooth.iterated(lay.ys, lay.offsets, m0, P0, im, iP, t_mat,
+                                                                    t_qm, t_Q, o_mat, o_qm, o_Q, icfg, fcfg)
+    out = (MVNStandard(lay.unpack_states(out_m, (nx,)), lay.unpack_states(out_P, (nx, nx))),)
+    if return_loglikelihood:
+        out += (lay.per_sequence(ell),)
+    if return_info:
+        out += ({"iterations": lay.per_sequence(iters), "flags": lay.per_sequence(flags)},)
+    return out[0] if len(out) == 1 else out
+
+
+def linearize(model, x, method, *, covariance_form="operators"):
     """Linearise ``model`` at ``x`` (one point or a batch) with ``method`` on the GPU.
 
-    Equivalent of ``method(model, x)`` in parsmooth/linearization/*.py."""
+    Equivalent of ``method(model, x)`` in parsmooth/linearization/*.py.  For a covariance-form
+    ``x`` (``MVNStandard``) the result is ``(F, Q, b)`` with ``Q`` a covariance: the reference's
+    covariance-form regression (parsmooth/linearization/_sigma_points.py:39-60, 81-86) in a
+    CUDA kernel, or (``covariance_form="factored"``) the square-root regression squared."""
     if isinstance(x, MVNStandard):
-        # the reference's covariance-form linearisation returns (F, Q, b) with Q a covariance
-        F, L, b = linearize(_model_to_sqrt(model), _std_to_sqrt(x), method)
-        return F, L @ L.transpose(-1, -2), b
+        if not _cov_form(covariance_form):
+            F, L, b = linearize(_model_to_sqrt(model), _std_to_sqrt(x), method)
+            return F, L @ L.transpose(-1, -2), b
+        return _linearize_std(model, x, method)
     method = resolve(method)
     dev = _device()
     m = torch.as_tensor(x.mean) if not isinstance(x.mean, torch.Tensor) else x.mean
@@ -780,6 +945,46 @@ def linearize(model, x, method):
     if single:
         return F[0], chol[0], b[0]
     return F.reshape(m.shape[:-1] + F.shape[1:]), chol.reshape(m.shape[:-1] + chol.shape[1:]), \
+        b.reshape(m.shape[:-1] + b.shape[1:])
+
+
+def _linearize_std(model, x, method):
+    """Covariance-form linearisation on the GPU (ss_linearize with SS_OPT_COVARIANCE_FORM)."""
+    method = resolve(method)
+    dev = _device()
+    m = torch.as_tensor(x.mean) if not isinstance(x.mean, torch.Tensor) else x.mean
+    dtype = m.dtype if m.dtype in _DT else torch.float32
+    single = m.ndim == 1
+    nx = int(m.shape[-1])
+    mm = _as(m, dtype, dev).reshape(-1, nx)
+    PP = _as(x.cov, dtype, dev).reshape(-1, nx, nx).contiguous()
+    if isinstance(model, ConditionalMomentsModel):
+        from .models import conditional_owner
+        fn = conditional_owner(model)
+    else:
+        fn = as_device_model(model.function)
+    d_out = fn.d_out
+    is_obs = not (d_out == nx and fn.kind not in (_lib.SS_MODEL_BEARINGS, _lib.SS_MODEL_POISSON_EXP))
+    fnm, mat, qm, Q = _model_tensors_std(model, nx, d_out, dtype, dev)
+    if is_obs:
+        fn_t, t_mat, t_qm, t_Q = _dummy_transition(nx, dtype, dev)
+        o = (fnm, mat, qm, Q)
+        ny = d_out
+    else:
+        fn_t, t_mat, t_qm, t_Q = fnm, mat, qm, Q
+        ny = _dummy_ny(nx)
+        o = _dummy_observation(nx, dtype, dev, ny)
+    lay_off = torch.zeros(2, dtype=torch.int64, device=dev)
+
+    class _L:
+        B, N, max_len = 1, 0, 0
+
+    icfg = _icfg(method, nx, ny, fn_t, o[0], _L, 0, 0, 0, [], cov=True)
+    F, cov_out, b = torch.ops.sqrtsmooth.linearize(mm, PP, lay_off, t_mat, t_qm, t_Q, o[1], o[2], o[3], icfg,
+                                                   _fcfg(method, fn_t, o[0]), 1 if is_obs else 0)
+    if single:
+        return F[0], cov_out[0], b[0]
+    return F.reshape(m.shape[:-1] + F.shape[1:]), cov_out.reshape(m.shape[:-1] + cov_out.shape[1:]), \
         b.reshape(m.shape[:-1] + b.shape[1:])
 
 

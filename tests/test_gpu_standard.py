@@ -1,6 +1,13 @@
-"""Covariance-form (MVNStandard) inputs, the reference's standard filter and smoother: the
-GPU factors them, computes in square-root form and returns covariances; results match the
-oracle's covariance-form path (parsmooth/parallel/_operators.py:7-40, 80-101)."""
+"""Covariance-form (MVNStandard) inputs, the reference's standard filter and smoother.
+
+By default they run the covariance-form kernels (csrc/ss_std.cuh): the reference's
+covariance-form linearisation, elements and operators (parsmooth/parallel/_operators.py:7-40,
+80-101; parsmooth/parallel/_filtering.py:64-97, 157-163; parsmooth/parallel/_smoothing.py:60-69).
+``covariance_form="factored"`` factors the covariances and runs the square-root kernels.  Both
+must match the oracle's covariance-form path in FP64.  In FP32 they are compared with the
+reference's own FP32 log-likelihoods of its robustness study."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -9,10 +16,12 @@ import oracle as O
 import sqrt_parallel_smoothers_gb300 as S
 from oracle import models as OM
 from sqrt_parallel_smoothers_gb300 import models as GM
-from tests._parity import assert_rel
+from tests._parity import assert_rel, bearings_pair, np_
 from tests._systems import lgssm
 
 pytestmark = pytest.mark.gpu
+
+FORMS = ["operators", "factored"]
 
 
 def _linear_std_pair(A, b, Q):
@@ -21,9 +30,23 @@ def _linear_std_pair(A, b, Q):
     return o, g
 
 
-@pytest.mark.parametrize("method", ["extended", "cubature"])
-def test_standard_filter_smoother_linear(method):
-    s = lgssm(4, 2, 60, seed=13)
+def _bearings_std(qc, qw, r, dtype=torch.float64):
+    Q, R = OM.bearings_noise(qc, qw, r, 0.01)
+    ot = O.FunctionalModel(O.models.CoordinatedTurn(0.01), O.MVNStandard(np.zeros(5), Q))
+    oo = O.FunctionalModel(O.models.Bearings((-1.5, 0.5), (1.0, 1.0)), O.MVNStandard(np.zeros(2), R))
+    gt = S.FunctionalModel(GM.CoordinatedTurn(0.01), S.MVNStandard(torch.zeros(5, dtype=dtype),
+                                                                    torch.as_tensor(Q, dtype=dtype)))
+    go = S.FunctionalModel(GM.Bearings((-1.5, 0.5), (1.0, 1.0)), S.MVNStandard(torch.zeros(2, dtype=dtype),
+                                                                               torch.as_tensor(R, dtype=dtype)))
+    return (ot, oo), (gt, go)
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("method", ["extended", "cubature", "unscented", "gauss_hermite"])
+@pytest.mark.parametrize("dims", [(4, 2), (1, 1), (3, 3), (5, 1)])
+def test_standard_filter_smoother_linear(method, form, dims):
+    nx, ny = dims
+    s = lgssm(nx, ny, 60, seed=13)
     ot, gt = _linear_std_pair(s["F"], s["b"], s["Q"])
     oo, go = _linear_std_pair(s["H"], s["c"], s["R"])
     x0 = s["x0"]
@@ -33,9 +56,9 @@ def test_standard_filter_smoother_linear(method):
     ref_s = O.methods.smoothing(ot, ref_f, getattr(O.linearization, method), None, True)
     gx0 = S.MVNStandard(torch.as_tensor(x0.mean), torch.as_tensor(x0.cov))
     filt, ell = S.filtering(torch.as_tensor(ys), gx0, gt, go, getattr(S.linearization, method), None,
-                            return_loglikelihood=True)
+                            return_loglikelihood=True, covariance_form=form)
     assert isinstance(filt, S.MVNStandard)
-    sm = S.smoothing(gt, filt, getattr(S.linearization, method))
+    sm = S.smoothing(gt, filt, getattr(S.linearization, method), covariance_form=form)
     assert isinstance(sm, S.MVNStandard)
     assert_rel(filt.mean, ref_f.mean, 1e-9, "filtered mean")
     assert_rel(filt.cov, ref_f.cov, 1e-9, "filtered cov")
@@ -44,18 +67,36 @@ def test_standard_filter_smoother_linear(method):
     assert_rel(sm.cov, ref_s.cov, 1e-9, "smoothed cov")
 
 
-def test_standard_iterated_bearings():
+@pytest.mark.parametrize("T", [1, 7, 64, 300])
+@pytest.mark.parametrize("chunk,group", [(1, 2), (3, 2), (16, 8)])
+def test_standard_scan_geometry(T, chunk, group):
+    """Covariance-form kernels at chunk/group sizes that force one to four scan levels."""
+    w = S.data.cv_workload(T, seed=0)
+    ot, gt = _linear_std_pair(w["F"], np.zeros(4), w["Q"])
+    oo, go = _linear_std_pair(w["H"], np.zeros(2), w["R"])
+    ys = w["ys"].astype(float)
+    P0 = w["P0"] @ w["P0"].T
+    ref, ref_ell = O.methods.filtering(ys, O.MVNStandard(w["m0"], P0), ot, oo, O.linearization.extended, None,
+                                       True, return_loglikelihood=True)
+    sm = O.methods.smoothing(ot, ref, O.linearization.extended)
+    x0 = S.MVNStandard(torch.as_tensor(w["m0"]), torch.as_tensor(P0))
+    res, ell = S.filtering(torch.as_tensor(ys), x0, gt, go, S.linearization.extended, return_loglikelihood=True,
+                           chunk=chunk, group=group)
+    assert_rel(res.mean, ref.mean, 1e-10, "filtered mean")
+    assert_rel(res.cov, ref.cov, 1e-10, "filtered cov")
+    assert abs(float(ell) - ref_ell) <= 1e-10 * abs(ref_ell)
+    sres = S.smoothing(gt, res, S.linearization.extended, chunk=chunk, group=group)
+    assert_rel(sres.mean, sm.mean, 1e-10, "smoothed mean")
+    assert_rel(sres.cov, sm.cov, 1e-10, "smoothed cov")
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_standard_iterated_bearings(form):
     """Covariance-form iterated cubature smoother on the bearings model (3 calls from the
     prior mean broadcast) against the oracle's covariance-form operators."""
     T = 80
     w = S.data.bearings_workload(T, seed=2)
-    Q, R = w["Q"], w["R"]
-    ot = O.FunctionalModel(O.models.CoordinatedTurn(0.01), O.MVNStandard(np.zeros(5), Q))
-    oo = O.FunctionalModel(O.models.Bearings((-1.5, 0.5), (1.0, 1.0)), O.MVNStandard(np.zeros(2), R))
-    gt = S.FunctionalModel(GM.CoordinatedTurn(0.01), S.MVNStandard(torch.zeros(5, dtype=torch.float64),
-                                                                    torch.as_tensor(Q)))
-    go = S.FunctionalModel(GM.Bearings((-1.5, 0.5), (1.0, 1.0)), S.MVNStandard(torch.zeros(2, dtype=torch.float64),
-                                                                               torch.as_tensor(R)))
+    (ot, oo), (gt, go) = _bearings_std(0.1, 0.5, 0.05)
     m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
     ys = w["ys"].astype(np.float64)
     nom = (np.repeat(m0[None], T + 1, 0), np.repeat(np.eye(5)[None], T + 1, 0))
@@ -66,26 +107,129 @@ def test_standard_iterated_bearings():
                                                                        torch.eye(5, dtype=torch.float64)),
                                     gt, go, S.linearization.cubature,
                                     S.MVNStandard(torch.as_tensor(nom[0]), torch.as_tensor(nom[1])),
-                                    criterion=lambda i, *_: i < 3, return_loglikelihood=True)
+                                    criterion=lambda i, *_: i < 3, return_loglikelihood=True, covariance_form=form)
     assert isinstance(res, S.MVNStandard)
     assert_rel(res.mean, ref.mean, 1e-8, "mean")
     assert_rel(res.cov, ref.cov, 1e-8, "cov")
     assert abs(float(ell) - ref_ell) <= 1e-8 * abs(ref_ell)
 
 
-def test_standard_linearize():
+def test_standard_iterated_ragged_default_nominal():
+    """A ragged batch from the reference's default nominal (one extra pass at zero means and
+    identity covariances), extended linearisation, FP64, against the oracle per sequence."""
+    lengths = np.array([5, 0, 33, 1, 70])
+    (ot, oo), (gt, go) = _bearings_std(0.1, 0.5, 0.05)
+    batch = S.data.bearings_batch(lengths, seed0=4)
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    x0 = S.MVNStandard(torch.as_tensor(m0), torch.eye(5, dtype=torch.float64))
+    res, ell, info = S.iterated_smoothing(torch.as_tensor(batch["ys"], dtype=torch.float64), x0, gt, go,
+                                          S.linearization.extended, None, criterion=lambda i, *_: i < 3,
+                                          return_loglikelihood=True, offsets=batch["offsets"], chunk=4, group=2,
+                                          return_info=True)
+    off = batch["offsets"]
+    for i, T in enumerate(lengths):
+        ys = batch["ys"][off[i]:off[i + 1]].astype(float)
+        ref, ref_ell = O.methods.iterated_smoothing(ys, O.MVNStandard(m0, np.eye(5)), ot, oo,
+                                                    O.linearization.extended, None, True,
+                                                    criterion=lambda k, *_: k < 3, return_loglikelihood=True)
+        a, b = off[i] + i, off[i + 1] + i + 1
+        assert_rel(res.mean[a:b], ref.mean, 1e-9, f"seq {i} mean")
+        assert_rel(res.cov[a:b], ref.cov, 1e-9, f"seq {i} cov")
+        if T > 0:
+            assert abs(float(ell[i]) - ref_ell) <= 1e-9 * max(1.0, abs(ref_ell))
+    assert int(info["flags"].abs().sum()) == 0
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_standard_linearize(form):
     rng = np.random.RandomState(0)
     Q, R = S.data.bearings_noise(0.1, 0.5, 0.05, 0.01)
     om = O.FunctionalModel(O.models.Bearings((-1.5, 0.5), (1.0, 1.0)), O.MVNStandard(np.zeros(2), R))
     gm = S.FunctionalModel(GM.Bearings((-1.5, 0.5), (1.0, 1.0)), S.MVNStandard(torch.zeros(2, dtype=torch.float64),
                                                                                torch.as_tensor(R)))
+    tm_o = O.FunctionalModel(O.models.CoordinatedTurn(0.01), O.MVNStandard(np.zeros(5), Q))
+    tm_g = S.FunctionalModel(GM.CoordinatedTurn(0.01), S.MVNStandard(torch.zeros(5, dtype=torch.float64),
+                                                                      torch.as_tensor(Q)))
     m = rng.randn(5)
     A = rng.randn(5, 5) * 0.3
     P = A @ A.T + 0.1 * np.eye(5)
-    for name in ("extended", "cubature"):
-        Fo, Qo, bo = getattr(O.linearization, name)(om, O.MVNStandard(m, P))
-        Fg, Qg, bg = S.linearize(gm, S.MVNStandard(torch.as_tensor(m), torch.as_tensor(P)),
-                                 getattr(S.linearization, name))
-        assert_rel(Fg, Fo, 1e-9, name + " F")
-        assert_rel(Qg, Qo, 1e-9, name + " Q")
-        assert_rel(bg, bo, 1e-9, name + " b")
+    for name in ("extended", "cubature", "unscented", "gauss_hermite"):
+        for o, g in ((om, gm), (tm_o, tm_g)):
+            Fo, Qo, bo = getattr(O.linearization, name)(o, O.MVNStandard(m, P))
+            Fg, Qg, bg = S.linearize(g, S.MVNStandard(torch.as_tensor(m), torch.as_tensor(P)),
+                                     getattr(S.linearization, name), covariance_form=form)
+            assert_rel(Fg, Fo, 1e-9, name + " F")
+            assert_rel(Qg, Qo, 1e-9, name + " Q")
+            assert_rel(bg, bo, 1e-9, name + " b")
+
+
+def test_standard_fp32_linear_close_to_fp64():
+    s = lgssm(3, 2, 200, seed=5)
+    ot, _ = _linear_std_pair(s["F"], s["b"], s["Q"])
+    oo, _ = _linear_std_pair(s["H"], s["c"], s["R"])
+    g32 = [S.FunctionalModel(GM.LinearModel(A), S.MVNStandard(torch.as_tensor(b, dtype=torch.float32),
+                                                              torch.as_tensor(Q, dtype=torch.float32)))
+           for A, b, Q in ((s["F"], s["b"], s["Q"]), (s["H"], s["c"], s["R"]))]
+    x0 = s["x0"]
+    ys = s["ys"].astype(np.float64)
+    ref_f = O.methods.filtering(ys, O.MVNStandard(x0.mean, x0.cov), ot, oo, O.linearization.cubature, None, True)
+    ref_s = O.methods.smoothing(ot, ref_f, O.linearization.cubature, None, True)
+    gx0 = S.MVNStandard(torch.as_tensor(x0.mean, dtype=torch.float32), torch.as_tensor(x0.cov, dtype=torch.float32))
+    sm = S.filter_smoother(torch.as_tensor(ys, dtype=torch.float32), gx0, g32[0], g32[1], S.linearization.cubature)
+    assert_rel(sm.mean, ref_s.mean, 2e-4, "smoothed mean")
+    assert_rel(sm.cov, ref_s.cov, 2e-4, "smoothed cov")
+
+
+def _robustness_run(lin, T, dtype, form):
+    """The reference's FP32 robustness study (notebooks/robustness_100runs.py): 20 runs, 20
+    iterated calls from the nominal (-1, -1, 6, 4, 2), prior (-4, -1, 2, 7, 3)."""
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "robustness_small.npz"))
+    runs = d["ys"].shape[0]
+    if form == "sqrt":
+        _, (gt, go) = bearings_pair(0.01, 0.1, 0.5)
+        x0 = S.MVNSqrt(torch.tensor([-4.0, -1.0, 2.0, 7.0, 3.0], dtype=dtype), torch.eye(5, dtype=dtype))
+        nom = S.MVNSqrt(torch.tensor([-1.0, -1.0, 6.0, 4.0, 2.0], dtype=dtype).expand(runs, T + 1, 5),
+                        torch.eye(5, dtype=dtype).expand(runs, T + 1, 5, 5))
+    else:
+        _, (gt, go) = _bearings_std(0.01, 0.1, 0.5, dtype)
+        x0 = S.MVNStandard(torch.tensor([-4.0, -1.0, 2.0, 7.0, 3.0], dtype=dtype), torch.eye(5, dtype=dtype))
+        nom = S.MVNStandard(torch.tensor([-1.0, -1.0, 6.0, 4.0, 2.0], dtype=dtype).expand(runs, T + 1, 5),
+                            torch.eye(5, dtype=dtype).expand(runs, T + 1, 5, 5))
+    _, ell = S.iterated_smoothing(torch.as_tensor(d["ys"][:, :T], dtype=dtype), x0, gt, go, lin, nom,
+                                  criterion=lambda i, *_: i < 20, return_loglikelihood=True)
+    return np_(ell), d
+
+
+def test_robustness_covariance_form_fp32_gpu():
+    """The reference's FP32 robustness study at T = 100: its covariance-form cubature smoother
+    returned a NaN log-likelihood on all 20 runs while its square-root form stayed finite
+    (notebooks/robustness_data/ell_float32_cubature_{std,sqrt}_100runs.npz).  The GPU's
+    covariance-form kernels, with the same formulas in FP32, stay finite on every run, and their
+    typical FP32 error against their own FP64 run is at rounding level, as for the square-root
+    kernels: the reference's failure is not reproduced (the scan here applies each element to
+    the prefix in state form, in another association than the reference's odd/even tree, and
+    the reference's JAX/XLA FP32 arithmetic on its GPU cannot be run here).  Kept as a record
+    of this behaviour."""
+    ell_std32, d = _robustness_run(S.linearization.cubature, 100, torch.float32, "std")
+    ell_std64, _ = _robustness_run(S.linearization.cubature, 100, torch.float64, "std")
+    ell_sqrt32, _ = _robustness_run(S.linearization.cubature, 100, torch.float32, "sqrt")
+    ell_sqrt64, _ = _robustness_run(S.linearization.cubature, 100, torch.float64, "sqrt")
+    ti = list(d["Ts"]).index(100)
+    assert np.isnan(d["ell_cubature_std"][ti]).all() and np.isfinite(d["ell_cubature"][ti]).all()
+    assert np.isfinite(ell_std32).all() and np.isfinite(ell_sqrt32).all() and np.isfinite(ell_std64).all()
+    # both forms agree in FP64 ...
+    assert np.max(np.abs(ell_std64 - ell_sqrt64) / np.abs(ell_sqrt64)) < 1e-5
+    # ... and their FP32 runs are typically at rounding level from it
+    assert np.median(np.abs(ell_std32 - ell_std64) / np.abs(ell_std64)) < 1e-5
+    assert np.median(np.abs(ell_sqrt32 - ell_sqrt64) / np.abs(ell_sqrt64)) < 1e-5
+
+
+@pytest.mark.parametrize("T", [20, 50, 100])
+def test_robustness_covariance_form_extended_gpu(T):
+    """The reference's FP32 covariance-form extended smoother does not fail; the GPU's
+    covariance-form kernels in FP32 agree with its log-likelihoods to 1e-4 on most runs."""
+    ell, d = _robustness_run(S.linearization.extended, T, torch.float32, "std")
+    g = d["ell_extended_std"][list(d["Ts"]).index(T)]
+    rel = np.abs(ell - g) / np.abs(g)
+    assert np.isfinite(ell).all()
+    assert np.mean(rel < 1e-4) >= 0.8, rel
