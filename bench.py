@@ -324,6 +324,31 @@ def time_plan(torch, plan, steps, warmup, flush=None, sampler=None):
     return [a.elapsed_time(b) for a, b in ev], clocks
 
 
+def measure_fp32_peak(torch):
+    """FP32 CUDA-core throughput of this GPU: a cuBLAS SGEMM of 8192^3 with TF32 off (best of 5,
+    CUDA events), TFLOP/s."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, device="cuda")
+        b = torch.randn(n, n, device="cuda")
+        c = a @ b
+        best = float("inf")
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b, out=c)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b, c
+        torch.cuda.empty_cache()
+        return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
 def position_rmse(mean, xs, offsets):
     """Per-sequence RMSE of smoothed (x, y) positions against the simulated truth."""
     out = []
@@ -343,6 +368,14 @@ ALG_BYTES_PER_STEP = {
     "filter_walk": 4 * (60 + 2 + 45),  # ... in, smoothing element out
     "smoother_walk": 4 * (45 + 20),  # smoothing element in, smoothed state out
 }
+# Whole filter-smoother pass, per timestep and call, at nx = 5, ny = 2 (FP32): the observation
+# (2 floats), the nominal state in (5 + 15), the smoothed state out (5 + 15) and the filtered
+# hand-off between the filter and the smoother written and read (2 x 20): 82 floats.
+PASS_ALG_BYTES_PER_STEP = 4 * (2 + 20 + 20 + 2 * 20)
+# Executed FP32 operations per timestep of each per-step kernel (flops: FFMA and FFMA2 count 2 and
+# 4, FADD/FMUL 1 and FADD2/FMUL2 2), from one ncu capture of this workload's kernels
+# (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul,ffma2,fadd2,fmul2}_pred_on.sum / timesteps).
+FP32_FLOPS_PER_STEP = {}
 # DRAM bytes (read + write) per timestep of each kernel, from one ncu capture of this workload
 # (bytes of one launch / 1,101,870 timesteps)
 TRAFFIC_BYTES_PER_STEP = {"lin": 314, "filter_leaf": 269, "filter_walk": 426, "smoother_walk": 257}
@@ -734,6 +767,31 @@ def gpu_arm(args):
                             "traffic": TRAFFIC_BYTES_PER_STEP[dom] * sum_T if dom in TRAFFIC_BYTES_PER_STEP else None,
                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
                             "alg_bytes_per_launch": alg * sum_T}
+    # the other side of the roofline: executed FP32 flops against the measured FP32 rate, per
+    # kernel and for the whole pass; and the whole pass's HBM fraction on its own minimal bytes
+    fp32_peak = measure_fp32_peak(torch)
+    pass_gbs = PASS_ALG_BYTES_PER_STEP * sum_T * N_ITER / (ms * 1e-3) / 1e9
+    line["roofline_pass"] = {
+        "hbm": {"alg_bytes_per_step_call": PASS_ALG_BYTES_PER_STEP, "achieved_gbs": pass_gbs,
+                "frac": pass_gbs / hbm_peak,
+                "definition": "observation, nominal in, smoothed out, filtered hand-off written and read: "
+                              "82 floats per timestep and call"},
+        "fp32_peak_tflops": fp32_peak,
+        "fp32_peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off, best of 5"}
+    if FP32_FLOPS_PER_STEP:
+        fl = {}
+        for k, f in FP32_FLOPS_PER_STEP.items():
+            if k in kern:
+                tf = f * sum_T / (kern[k]["avg_ms"] * 1e-3) / 1e12
+                fl[k] = {"flops_per_step": f, "achieved_tflops": tf, "frac": tf / fp32_peak}
+        tot_f = sum(FP32_FLOPS_PER_STEP.values())
+        pass_tf = tot_f * sum_T * N_ITER / (ms * 1e-3) / 1e12
+        line["roofline_pass"]["fp32"] = {"flops_per_step_call": tot_f, "achieved_tflops": pass_tf,
+                                         "frac": pass_tf / fp32_peak, "kernels": fl,
+                                         "source": "executed FP32 operations of the per-step kernels (ncu)"}
+        if dom in fl:
+            line["roofline_fp32"] = {"kernel": dom, "bound": "fp32", "achieved": fl[dom]["achieved_tflops"],
+                                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": fl[dom]["frac"]}
     line["kernels"] = kern
     if args.only_main:
         print(json.dumps(line), flush=True)
