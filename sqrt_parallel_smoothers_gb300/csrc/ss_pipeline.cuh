@@ -859,6 +859,149 @@ __global__ void __launch_bounds__(128) sample_kernel(ScanArgs<R> a, int S, const
   }
 }
 
+// Parallel in time, for few draws of long sequences.  The backward recursion is
+// a composition of affine maps x_t = E_t x_{t+1} + (g_t + D_t e_t), associative
+// as in the reference's _par_sampling scan (parsmooth/_pathwise_sampler.py:13-38).
+// The sequence is cut into chunks (geometry g, one level): sample_leaf_kernel
+// composes each chunk's maps into x_{t0} = A x_{t1} + c per (chunk, draw),
+// sample_top_kernel walks the chunk maps of each (sequence, draw) backwards from
+// x_T and stores every chunk's end state, and sample_walk_kernel replays each
+// chunk from its end state.  One thread per (chunk, draw) or (sequence, draw);
+// maps hold NX * NX + NX values and ends NX values per (chunk, draw).
+template <typename R, int NX>
+__global__ void __launch_bounds__(128) sample_leaf_kernel(Geo g, const R* __restrict__ selem, int S,
+                                                          const R* __restrict__ eps, R* __restrict__ maps) {
+  typedef Rec<R, NX, 1> Q;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.lvl[1][g.B] * (int64_t)S) return;
+  const int64_t j = k / S, smp = k - j * S;
+  int64_t i, t0, t1;
+  chunk_of(g, j, i, t0, t1);
+  const int64_t base = g.off[i], s0 = base + i;
+  R A[NX][NX], c[NX];
+  SS_UNROLL
+  for (int r = 0; r < NX; ++r) {
+    c[r] = R(0);
+    SS_UNROLL
+    for (int q = 0; q < NX; ++q) A[r][q] = (r == q) ? R(1) : R(0);
+  }
+  for (int64_t t = t1 - 1; t >= t0; --t) {
+    SElem<R, NX> se;
+    load_se<R, NX>(selem + (base + t) * Q::SE_P, se);
+    const R* e = eps + ((s0 + t) * S + smp) * NX;
+    R nA[NX][NX], nc[NX];
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = se.g[r];
+      SS_UNROLL
+      for (int q = 0; q < NX; ++q) v += se.E[r][q] * c[q];
+      SS_UNROLL
+      for (int q = 0; q <= r; ++q) v += se.D[r][q] * e[q];
+      nc[r] = v;
+      SS_UNROLL
+      for (int q = 0; q < NX; ++q) {
+        R a = R(0);
+        SS_UNROLL
+        for (int p = 0; p < NX; ++p) a += se.E[r][p] * A[p][q];
+        nA[r][q] = a;
+      }
+    }
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      c[r] = nc[r];
+      SS_UNROLL
+      for (int q = 0; q < NX; ++q) A[r][q] = nA[r][q];
+    }
+  }
+  R* o = maps + k * (NX * NX + NX);
+  SS_UNROLL
+  for (int r = 0; r < NX; ++r) {
+    o[NX * NX + r] = c[r];
+    SS_UNROLL
+    for (int q = 0; q < NX; ++q) o[r * NX + q] = A[r][q];
+  }
+}
+
+template <typename R, int NX>
+__global__ void __launch_bounds__(128) sample_top_kernel(Geo g, const R* __restrict__ fT, int S,
+                                                         const R* __restrict__ eps, const R* __restrict__ maps,
+                                                         R* __restrict__ ends, R* __restrict__ out) {
+  typedef Rec<R, NX, 1> Q;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.B * (int64_t)S) return;
+  const int64_t i = k / S, smp = k - i * S;
+  const int64_t T = g.off[i + 1] - g.off[i];
+  const int64_t s0 = g.off[i] + i;
+  State<R, NX> f;
+  load_st<R, NX>(fT + i * Q::ST_P, f);
+  R x[NX];
+  {
+    const R* e = eps + ((s0 + T) * S + smp) * NX;
+    R* o = out + ((s0 + T) * S + smp) * NX;
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = f.m[r];
+      SS_UNROLL
+      for (int c = 0; c <= r; ++c) v += f.L[r][c] * e[c];
+      x[r] = v;
+      o[r] = v;
+    }
+  }
+  for (int64_t j = g.lvl[1][i + 1] - 1; j >= g.lvl[1][i]; --j) {
+    const int64_t kk = j * S + smp;
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) ends[kk * NX + r] = x[r];
+    const R* mp = maps + kk * (NX * NX + NX);
+    R xn[NX];
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = mp[NX * NX + r];
+      SS_UNROLL
+      for (int q = 0; q < NX; ++q) v += mp[r * NX + q] * x[q];
+      xn[r] = v;
+    }
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) x[r] = xn[r];
+  }
+}
+
+template <typename R, int NX>
+__global__ void __launch_bounds__(128) sample_walk_kernel(Geo g, const R* __restrict__ selem, int S,
+                                                          const R* __restrict__ eps, const R* __restrict__ ends,
+                                                          R* __restrict__ out) {
+  typedef Rec<R, NX, 1> Q;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.lvl[1][g.B] * (int64_t)S) return;
+  const int64_t j = k / S, smp = k - j * S;
+  int64_t i, t0, t1;
+  chunk_of(g, j, i, t0, t1);
+  const int64_t base = g.off[i], s0 = base + i;
+  R x[NX];
+  SS_UNROLL
+  for (int r = 0; r < NX; ++r) x[r] = ends[k * NX + r];
+  for (int64_t t = t1 - 1; t >= t0; --t) {
+    SElem<R, NX> se;
+    load_se<R, NX>(selem + (base + t) * Q::SE_P, se);
+    const R* e = eps + ((s0 + t) * S + smp) * NX;
+    R* o = out + ((s0 + t) * S + smp) * NX;
+    R xn[NX];
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      R v = se.g[r];
+      SS_UNROLL
+      for (int c = 0; c < NX; ++c) v += se.E[r][c] * x[c];
+      SS_UNROLL
+      for (int c = 0; c <= r; ++c) v += se.D[r][c] * e[c];
+      xn[r] = v;
+    }
+    SS_UNROLL
+    for (int r = 0; r < NX; ++r) {
+      x[r] = xn[r];
+      o[r] = xn[r];
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- finishing kernels
 
 // Per-sequence log-likelihood: sum of chunk partials plus the constant

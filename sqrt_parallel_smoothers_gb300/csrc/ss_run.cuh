@@ -1,5 +1,6 @@
 // Host orchestration of one API call for a compile-time (R, NX, NY).
 #pragma once
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -477,10 +478,36 @@ struct Runner {
     sa.in_L = static_cast<const R*>(c.in_L);
     SS_LAUNCH("smoother_leaf", st, smoother_leaf_kernel<R, NX, NY><<<grid_for(y.items[1], 128), 128, 0, st>>>(sa));
     SS_LAUNCH("last_state", st, last_state_kernel<R, NX><<<grid_for(p.batch, 128), 128, 0, st>>>(sa));
-    const int64_t n = p.batch * (int64_t)c.n_samples;
-    SS_LAUNCH("sample", st, sample_kernel<R, NX><<<grid_for(n, 128), 128, 0, st>>>(sa, c.n_samples,
-                                                                                     static_cast<const R*>(c.eps),
-                                                                                     static_cast<R*>(c.out_m)));
+    const int S = c.n_samples;
+    const int64_t n = p.batch * (int64_t)S;
+    const R* eps = static_cast<const R*>(c.eps);
+    R* out = static_cast<R*>(c.out_m);
+    // Few independent walkers on long sequences: the parallel-in-time sampler, with chunks of
+    // about sqrt(T) steps (three chains of that length instead of one of T).  Its chunk maps
+    // and end states go to the level-1 summary regions of the workspace, which sampling does
+    // not otherwise use, and its one-level geometry to the level offsets, which the smoother
+    // leaf has finished with (stream order); when they do not fit, the per-walker kernel runs.
+    constexpr int64_t SAMPLE_SERIAL_MIN = 16384;
+    if (n < SAMPLE_SERIAL_MIN && p.max_len >= 64) {
+      const int cs = std::max(16, (int)std::ceil(std::sqrt((double)p.max_len)));
+      const int64_t items = (p.total_steps + cs - 1) / cs + p.batch;
+      const bool fits = (size_t)(items * S) * (NX * NX + NX) <= (size_t)y.items[1] * Q::FE_P &&
+                        (size_t)(items * S) * NX <= (size_t)y.items[1] * Q::ST_P;
+      if (fits) {
+        Geo gs = geo;
+        gs.C = cs;
+        gs.L = 1;
+        for (int l = 2; l <= MAX_LEVELS; ++l) gs.lvl[l] = nullptr;
+        SS_LAUNCH("plan", st, plan_kernel<512><<<1, 512, 0, st>>>(gs, at<int64_t>(y.lvl), (int64_t)y.lvl_stride));
+        R* maps = at<R>(y.fsum[1]);
+        R* ends = at<R>(y.fst[1]);
+        SS_LAUNCH("sample_leaf", st, sample_leaf_kernel<R, NX><<<grid_for(items * S, 128), 128, 0, st>>>(gs, sa.selem, S, eps, maps));
+        SS_LAUNCH("sample_top", st, sample_top_kernel<R, NX><<<grid_for(n, 128), 128, 0, st>>>(gs, sa.fT, S, eps, maps, ends, out));
+        SS_LAUNCH("sample_walk", st, sample_walk_kernel<R, NX><<<grid_for(items * S, 128), 128, 0, st>>>(gs, sa.selem, S, eps, ends, out));
+        return SS_OK;
+      }
+    }
+    SS_LAUNCH("sample", st, sample_kernel<R, NX><<<grid_for(n, 128), 128, 0, st>>>(sa, S, eps, out));
     return SS_OK;
   }
 

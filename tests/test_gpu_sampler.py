@@ -77,3 +77,52 @@ def test_sampler_moments_match_the_smoother():
     d = xs - mean[:, None]
     emp = torch.einsum("tsi,tsj->tij", d, d) / (n - 1)
     assert float((emp - cov_s).abs().max()) <= 0.05 * float(cov_s.abs().max())
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-9), (torch.float32, 2e-3)])
+def test_sampler_parallel_in_time_long_sequence(dtype, tol):
+    """Few draws of a long sequence take the parallel-in-time sampler (chunk maps composed,
+    scanned and replayed, as the reference's _par_sampling composes its affine maps); the
+    draws equal the oracle's for the same normals and the same nominal."""
+    (ot, oo), (gt, go) = bearings_pair(0.1, 0.5, 0.05)
+    T, n = 3000, 2
+    w = S.data.bearings_batch(np.array([T]), seed0=4)
+    ys = w["ys"].astype(np.float64)
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    filt = O.methods.filtering(ys, O.MVNSqrt(m0, np.eye(5)), ot, oo, O.linearization.extended, None, True)
+    nom = O.methods.smoothing(ot, filt, O.linearization.extended, None, True)
+    eps = np.random.RandomState(2).randn(T + 1, n, 5)
+    ref = OS.sampling(eps, ot, filt, O.linearization.extended, nom)
+    got = S.sampling(None, n, gt, S.MVNSqrt(torch.as_tensor(filt.mean, dtype=dtype),
+                                            torch.as_tensor(filt.chol, dtype=dtype)),
+                     S.linearization.extended, S.MVNSqrt(torch.as_tensor(nom.mean, dtype=dtype),
+                                                         torch.as_tensor(nom.chol, dtype=dtype)),
+                     eps=torch.as_tensor(eps, dtype=dtype))
+    assert got.shape == (T + 1, n, 5)
+    assert_rel(got, ref, tol, "samples")
+
+
+def test_sampler_parallel_in_time_ragged_batch():
+    rng = np.random.RandomState(5)
+    F = np.array([[1.0, 0.1], [0.0, 1.0]])
+    ot, gt = linear_pair(F, np.zeros(2), np.linalg.cholesky(0.1 * np.eye(2)))
+    oo, go = linear_pair(np.eye(1, 2), np.zeros(1), np.linalg.cholesky(0.5 * np.eye(1)))
+    lengths = np.array([500, 0, 130, 64, 1])
+    Tm, n = int(lengths.max()), 3
+    ys = rng.randn(len(lengths), Tm, 1)
+    eps = rng.randn(len(lengths), Tm + 1, n, 2)
+    fm = np.zeros((len(lengths), Tm + 1, 2))
+    fL = np.zeros((len(lengths), Tm + 1, 2, 2))
+    refs = []
+    for i, T in enumerate(lengths):
+        f = O.methods.filtering(ys[i, :T], O.MVNSqrt(np.zeros(2), np.eye(2)), ot, oo, O.linearization.extended,
+                                None, True)
+        fm[i, :T + 1], fL[i, :T + 1] = f.mean, f.chol
+        nom = O.MVNSqrt(np.zeros((T + 1, 2)), np.repeat(np.eye(2)[None], T + 1, 0))
+        refs.append(OS.sampling(eps[i, :T + 1], ot, f, O.linearization.extended, nom))
+    nom_g = S.MVNSqrt(torch.zeros(len(lengths), Tm + 1, 2, dtype=torch.float64),
+                      torch.eye(2, dtype=torch.float64).expand(len(lengths), Tm + 1, 2, 2).contiguous())
+    got = S.sampling(None, n, gt, S.MVNSqrt(torch.as_tensor(fm), torch.as_tensor(fL)), S.linearization.extended,
+                     nom_g, lengths=lengths, eps=eps)
+    for i, T in enumerate(lengths):
+        assert_rel(got[i, :T + 1], refs[i], 1e-10, f"seq {i}")
