@@ -530,6 +530,34 @@ def population_section(torch, S, flush):
     return out
 
 
+def sampler_section(torch, S, flush, T=100_000):
+    """Pathwise posterior sampling (parsmooth.sampling) of one draw of one bearings sequence of
+    T = 1e5 steps, FP32, at the smoothed trajectory: the parallel-in-time sampler (with one
+    walker, the per-walker kernel would be one thread stepping through all T steps).  Timed
+    with CUDA events around the whole call (its linearisation, the smoothing elements and the
+    draw), median of 5 after 2 warm-up calls."""
+    one = S.data.bearings_batch(np.array([T]), qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=40_000)
+    dt = torch.float32
+    tm, om = models(torch, S, dt)
+    x0 = S.MVNSqrt(torch.as_tensor(PRIOR_M0, dtype=dt), torch.eye(5, dtype=dt))
+    filt = S.filtering(torch.as_tensor(one["ys"], dtype=dt), x0, tm, om, S.linearization.cubature)
+    nom = S.smoothing(tm, filt, S.linearization.cubature)
+    eps = torch.randn((T + 1, 1, 5), dtype=dt, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    ms = []
+    for k in range(7):
+        flush.add_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        xs = S.sampling(None, 1, tm, filt, S.linearization.cubature, nom, eps=eps)
+        e1.record()
+        torch.cuda.synchronize()
+        if k >= 2:
+            ms.append(e0.elapsed_time(e1))
+    return {"T": T, "samples": 1, "dtype": "f32", "ms": float(np.median(ms)),
+            "timesteps_per_s": T / (float(np.median(ms)) * 1e-3), "finite": bool(torch.isfinite(xs).all()),
+            "path": "parallel in time (chunks of ~sqrt(T) steps)"}
+
+
 def sweep_section(torch, S, flush):
     """Single-sequence bearings smoother (10 calls from the prior mean broadcast) for
     T = 1e2 .. 1e5, FP64 then FP32: timesteps/s and the FP32 position RMSE against FP64's."""
@@ -843,6 +871,7 @@ def gpu_arm(args):
         line["population"] = population_section(torch, S, flush)
         line["published_runtime"] = published_runtime_section(torch, S, flush)
         line["sweep_T"] = sweep_section(torch, S, flush)
+        line["sampler"] = sampler_section(torch, S, flush)
         line["large_state"] = large_state_section(torch, S, flush)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

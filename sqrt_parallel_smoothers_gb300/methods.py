@@ -514,7 +514,10 @@ def _cov_form(covariance_form):
 def _model_tensors_std(model, d_in, d_out, dtype, device):
     """Device model with its noise mean and covariance (covariance-form kernels)."""
     if isinstance(model, ConditionalMomentsModel):
-        return _model_tensors(model, d_in, d_out, dtype, device)   # the model gives its conditional covariances
+        # the device model's constant noise enters as its covariance (conditional observation
+        # models compute theirs per point in the kernel and ignore it)
+        fn, mat, qm, qL = _model_tensors(model, d_in, d_out, dtype, device)
+        return fn, mat, qm, (qL @ qL.transpose(-1, -2)).contiguous()
     if not isinstance(model, FunctionalModel):
         raise TypeError(f"expected a FunctionalModel, got {type(model).__name__}")
     fn = as_device_model(model.function)
