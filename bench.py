@@ -373,9 +373,10 @@ ALG_BYTES_PER_STEP = {
 # hand-off between the filter and the smoother written and read (2 x 20): 82 floats.
 PASS_ALG_BYTES_PER_STEP = 4 * (2 + 20 + 20 + 2 * 20)
 # Executed FP32 operations per timestep of each per-step kernel (flops: FFMA and FFMA2 count 2 and
-# 4, FADD/FMUL 1 and FADD2/FMUL2 2), from one ncu capture of this workload's kernels
-# (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul,ffma2,fadd2,fmul2}_pred_on.sum / timesteps).
-FP32_FLOPS_PER_STEP = {}
+# 4, FADD/FMUL 1 and FADD2/FMUL2 2), from one ncu capture of the first call of this workload's
+# kernels on its first 128 sequences (sm__sass_thread_inst_executed_op_{ffma,fadd,fmul,ffma2,
+# fadd2,fmul2}_pred_on.sum / 133,357 timesteps; no FFMA2/FADD2/FMUL2 were executed).
+FP32_FLOPS_PER_STEP = {"lin": 1761, "filter_leaf": 1868, "filter_walk": 3103, "smoother_walk": 555}
 # DRAM bytes (read + write) per timestep of each kernel, from one ncu capture of this workload
 # (bytes of one launch / 1,101,870 timesteps)
 TRAFFIC_BYTES_PER_STEP = {"lin": 314, "filter_leaf": 269, "filter_walk": 426, "smoother_walk": 257}

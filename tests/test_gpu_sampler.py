@@ -93,10 +93,10 @@ def test_sampler_parallel_in_time_long_sequence(dtype, tol):
     nom = O.methods.smoothing(ot, filt, O.linearization.extended, None, True)
     eps = np.random.RandomState(2).randn(T + 1, n, 5)
     ref = OS.sampling(eps, ot, filt, O.linearization.extended, nom)
-    got = S.sampling(None, n, gt, S.MVNSqrt(torch.as_tensor(filt.mean, dtype=dtype),
-                                            torch.as_tensor(filt.chol, dtype=dtype)),
-                     S.linearization.extended, S.MVNSqrt(torch.as_tensor(nom.mean, dtype=dtype),
-                                                         torch.as_tensor(nom.chol, dtype=dtype)),
+    got = S.sampling(None, n, gt, S.MVNSqrt(torch.as_tensor(np.ascontiguousarray(filt.mean), dtype=dtype),
+                                            torch.as_tensor(np.ascontiguousarray(filt.chol), dtype=dtype)),
+                     S.linearization.extended, S.MVNSqrt(torch.as_tensor(np.ascontiguousarray(nom.mean), dtype=dtype),
+                                                         torch.as_tensor(np.ascontiguousarray(nom.chol), dtype=dtype)),
                      eps=torch.as_tensor(eps, dtype=dtype))
     assert got.shape == (T + 1, n, 5)
     assert_rel(got, ref, tol, "samples")
