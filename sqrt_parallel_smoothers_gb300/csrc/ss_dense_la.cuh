@@ -307,11 +307,90 @@ SS_DEV void tria(R* M, R* vb) {
 
 // ----------------------------------------------------------------------------- products
 
+// FP32 products on the tensor cores: warp-level mma.sync m16n8k8 with TF32
+// operands and FP32 accumulation, each operand split into a TF32 high part and
+// a TF32 remainder (x = hi + lo) and the product accumulated as
+// lo*hi + hi*lo + hi*hi ("3xTF32"): the dropped lo*lo term is below FP32
+// rounding, so the result has FP32 accuracy while the multiply-adds run on the
+// tensor pipe.  Fragment layout of m16n8k8 (g = lane / 4, t = lane % 4):
+// A (16 x 8) a0 (g, t), a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4);
+// B (8 x 8) b0 (k = t, n = g), b1 (k = t + 4, n = g);
+// C (16 x 8) c0, c1 (g, 2t, 2t + 1), c2, c3 (g + 8, 2t, 2t + 1).
+SS_DEV uint32_t tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+SS_DEV void tf32_split(float x, uint32_t& hi, uint32_t& lo) {
+  hi = tf32_hi(x);
+  lo = tf32_hi(x - __uint_as_float(hi));
+}
+SS_DEV void mma_tf32(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, "
+               "{%8, %9}, {%0, %1, %2, %3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int M, int K, int N, bool TA, bool TB, int LDA, int LDB, int LDC, bool LB>
+SS_DEV void mm_tc(float* C, const float* A, const float* B, float alpha, bool acc) {
+  static_assert(M % 16 == 0 && K % 8 == 0 && N % 8 == 0, "tensor-core tiles");
+  constexpr int KT = K / 8;
+  const int lane = lane_id();
+  const int g = lane >> 2, t = lane & 3;
+  auto a_at = [&](int m, int k) -> float { return TA ? A[k * LDA + m] : A[m * LDA + k]; };
+  auto b_at = [&](int k, int n) -> float {
+    if (LB && n > k) return 0.0f;
+    return TB ? B[n * LDB + k] : B[k * LDB + n];
+  };
+#pragma unroll 1
+  for (int m0 = 0; m0 < M; m0 += 16) {
+    uint32_t ah[KT][4], al[KT][4];
+    SS_UNROLL
+    for (int kt = 0; kt < KT; ++kt) {
+      const int k0 = kt * 8;
+      tf32_split(a_at(m0 + g, k0 + t), ah[kt][0], al[kt][0]);
+      tf32_split(a_at(m0 + g + 8, k0 + t), ah[kt][1], al[kt][1]);
+      tf32_split(a_at(m0 + g, k0 + t + 4), ah[kt][2], al[kt][2]);
+      tf32_split(a_at(m0 + g + 8, k0 + t + 4), ah[kt][3], al[kt][3]);
+    }
+#pragma unroll 1
+    for (int n0 = 0; n0 < N; n0 += 8) {
+      float d[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      SS_UNROLL
+      for (int kt = 0; kt < KT; ++kt) {
+        const int k0 = kt * 8;
+        uint32_t bh[2], bl[2];
+        tf32_split(b_at(k0 + t, n0 + g), bh[0], bl[0]);
+        tf32_split(b_at(k0 + t + 4, n0 + g), bh[1], bl[1]);
+        mma_tf32(d, al[kt], bh);
+        mma_tf32(d, ah[kt], bl);
+        mma_tf32(d, ah[kt], bh);
+      }
+      const int r0 = m0 + g, c0 = n0 + 2 * t;
+      float* p0 = C + r0 * LDC + c0;
+      float* p1 = C + (r0 + 8) * LDC + c0;
+      const float o0 = acc ? p0[0] : 0.0f, o1 = acc ? p0[1] : 0.0f;
+      const float o2 = acc ? p1[0] : 0.0f, o3 = acc ? p1[1] : 0.0f;
+      p0[0] = o0 + alpha * d[0];
+      p0[1] = o1 + alpha * d[1];
+      p1[0] = o2 + alpha * d[2];
+      p1[1] = o3 + alpha * d[3];
+    }
+  }
+  __syncwarp();
+}
+
 // C = alpha op(A) op(B) (+ C when acc), C: M x N, op(A): M x K, op(B): K x N,
 // op(X) = X^T when the flag is set.
 // LB: B is lower triangular (its strict upper part is skipped).
+// FP32 shapes that tile into 16 x 8 x 8 run on the tensor cores (mm_tc).
 template <typename R, int M, int K, int N, bool TA, bool TB, int LDA, int LDB, int LDC, bool LB = false>
 SS_DEV void mm(R* C, const R* A, const R* B, R alpha = R(1), bool acc = false) {
+  if constexpr (std::is_same<R, float>::value && M % 16 == 0 && K % 8 == 0 && N % 8 == 0) {
+    mm_tc<M, K, N, TA, TB, LDA, LDB, LDC, LB>(C, A, B, alpha, acc);
+    return;
+  }
   constexpr int W = Vec<R>::n;
   constexpr int KP = Pad<R, K>::n, NP = Pad<R, N>::n;
   const int lane = lane_id();
