@@ -641,6 +641,18 @@ def large_state_section(torch, S, flush, chunk=32, T=131_072, compare=True):
     launches = plan.launches_per_run
     del plan
     torch.cuda.empty_cache()
+    # the general batch: every sequence's factor recursion computed separately
+    S.set_large_state_options(per_sequence_covariance=True)
+    try:
+        plan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None,
+                                      criterion=S.FixedIterations(9), offsets=offsets, chunk=chunk, group=8,
+                                      graph=True)
+        ms_ps, _ = time_plan(torch, plan, 2, 1, flush)
+        del plan
+    finally:
+        S.set_large_state_options(per_sequence_covariance=False)
+    torch.cuda.empty_cache()
+    per_seq_ms = float(np.median(ms_ps))
     pplan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None, criterion=S.FixedIterations(9),
                                    offsets=offsets, chunk=chunk, group=8, graph=True, profile=True)
     pplan.run()
@@ -657,14 +669,18 @@ def large_state_section(torch, S, flush, chunk=32, T=131_072, compare=True):
         per_launch_ms = kern[dom]["total_ms"] / kern[dom]["launches"]
         flops = LARGE_FLOPS_FACTOR[dom] * T + LARGE_FLOPS_VECTOR[dom] * B * T
         ach = flops / (per_launch_ms * 1e-3) / 1e12
-        roof = {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": 80.5, "unit": "TFLOP/s", "frac": ach / 80.5,
-                "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 x 2.07 GHz); no measured FP32 peak",
+        peak = measure_fp32_peak(torch)
+        roof = {"kernel": dom, "bound": "fp32", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "peak_source": "measured here: cuBLAS SGEMM 8192^3, TF32 off (the kernels' factor products run "
+                               "on the tensor cores as 3xTF32 mma.sync, the Householder steps on the FP32 pipe)",
                 "alg_flops_per_launch": flops,
                 "flops_model": "factor recursion once per time step (shared covariance), vectors per sequence step"}
     out = {"workload": f"linear nx=32 ny=16 (F = 0.98 Haar, Q = L L^T/nx, H ~ N(0, 1/nx), R = 0.1 I), B=16, "
                        f"T={T}, FP32, 10 filter-smoother passes, chunk {chunk}, one CUDA graph",
            "mode": "shared covariance (one prior, equal lengths): factors once per time step, means per sequence",
            "ms_per_step": step_ms, "timesteps_per_s": B * T / (step_ms * 1e-3), "gpu_launches": launches,
+           "per_sequence_covariance": {"ms_per_step": per_seq_ms, "timesteps_per_s": B * T / (per_seq_ms * 1e-3),
+                                       "mode": "every sequence's factors computed separately (the general batch)"},
            "kernels": kern, "roofline": roof}
     if not compare:
         return out
