@@ -382,10 +382,26 @@ FP32_FLOPS_PER_STEP = {"lin": 1761, "filter_leaf": 1868, "filter_walk": 3103, "s
 TRAFFIC_BYTES_PER_STEP = {"lin": 314, "filter_leaf": 269, "filter_walk": 426, "smoother_walk": 257}
 
 
+def _timed(torch, flush, fn, reps=3):
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        flush.add_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    return float(np.median(times)) * 1e3, out
+
+
 def adjoint_section(torch, S, flush):
     """Gradient of the batch pseudo-log-likelihood w.r.t. (s1x, s1y, log q, log sigma): bearings model,
-    B = 64 sequences of T = 5000, FP32 tangent-linear filter, checked against central differences
-    (h = 1e-3) of the same filter in FP64."""
+    B = 64 sequences of T = 5000, FP32, from the reverse pass (filter, smoother scan, per-step
+    contraction) and from the tangent-linear filter (one pass per parameter), both checked against
+    central differences (h = 1e-3) of the FP64 filter.  Then p = 32 (every entry of F and of the
+    process-noise square root of the constant-velocity model, nx = 4) on the same batch shape."""
     B, T = 64, 5000
     batch = S.data.bearings_batch(np.full(B, T), qc=QC, qw=QW, sigma=SIGMA, dt=DT, seed0=20_000)
     Q1, _ = S.data.bearings_noise(1.0, QW / QC, SIGMA, DT)
@@ -394,35 +410,75 @@ def adjoint_section(torch, S, flush):
     x0 = S.MVNSqrt(m0, torch.eye(5, dtype=torch.float64))
     n_states = B * (T + 1)
     nom = S.MVNSqrt(m0.expand(n_states, 5).contiguous(), torch.eye(5, dtype=torch.float64).expand(n_states, 5, 5))
+    ys32 = torch.as_tensor(batch["ys"], dtype=torch.float32)
 
-    def ell_grad(theta, dtype):
+    def ell_grad(theta, ys, mode):
         th = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
-        ell = S.BearingsLogLikelihood.apply(th, torch.as_tensor(batch["ys"], dtype=dtype), x0, nom, Q1, DT, S2,
-                                            S.linearization.cubature, None, batch["offsets"])
+        ell = S.BearingsLogLikelihood.apply(th, ys, x0, nom, Q1, DT, S2, S.linearization.cubature, None,
+                                            batch["offsets"], 0, mode)
         ell.backward()
         return float(ell.detach()), th.grad.numpy()
 
-    ell_grad(theta0, torch.float32)
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(3):
-        flush.add_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ell32, g32 = ell_grad(theta0, torch.float32)
-        torch.cuda.synchronize()
-        times.append(time.perf_counter() - t0)
+    ms_rev, (ell32, g_rev) = _timed(torch, flush, lambda: ell_grad(theta0, ys32, "reverse"))
+    ms_tan, (_, g_tan) = _timed(torch, flush, lambda: ell_grad(theta0, ys32, "tangent"))
     h = 1e-3
-    fd = []
-    for k in range(4):
-        e = np.zeros(4)
-        e[k] = h
-        fd.append((ell_grad(theta0 + e, torch.float64)[0] - ell_grad(theta0 - e, torch.float64)[0]) / (2 * h))
-    fd = np.array(fd)
-    rel = np.abs(g32 - fd) / np.abs(fd)
-    return {"B": B, "T": T, "dtype": "f32", "ms": float(np.median(times)) * 1e3, "ell": ell32,
-            "grad": g32.tolist(), "fd_grad_fp64": fd.tolist(), "rel_err": rel.tolist(),
-            "max_rel_err": float(np.max(rel)), "method": "tangent-linear filter, one pass per parameter"}
+    ys64 = torch.as_tensor(batch["ys"], dtype=torch.float64)
+    fd = np.array([(ell_grad(theta0 + h * e, ys64, "tangent")[0] - ell_grad(theta0 - h * e, ys64, "tangent")[0])
+                   / (2 * h) for e in np.eye(4)])
+    rel_rev = np.abs(g_rev - fd) / np.abs(fd)
+    rel_tan = np.abs(g_tan - fd) / np.abs(fd)
+    out = {"B": B, "T": T, "dtype": "f32", "ms": ms_rev, "ell": ell32, "grad": g_rev.tolist(),
+           "fd_grad_fp64": fd.tolist(), "rel_err": rel_rev.tolist(), "max_rel_err": float(np.max(rel_rev)),
+           "method": "reverse pass: filter + smoother scan + per-step contraction of the smoothed moments "
+                     "(Fisher's identity), cost independent of the parameter count",
+           "tangent": {"ms": ms_tan, "grad": g_tan.tolist(), "max_rel_err": float(np.max(rel_tan)),
+                       "method": "tangent-linear filter, one pass per parameter"}}
+    out["p32"] = _adjoint_p32(torch, S, flush, B, T)
+    return out
+
+
+def _adjoint_p32(torch, S, flush, B, T):
+    """d ell / d (F, L_Q) of the constant-velocity model (nx = 4, ny = 2, dt = 0.1, q = 0.1,
+    R = 0.5 I): 16 + 16 parameters, B sequences of T steps, FP32; the reverse pass against the
+    tangent-linear filter run four directions at a time."""
+    F, Q, H, R = S.data.cv_model()
+    ys = np.concatenate([S.data.lgssm_data(np.zeros(4), F, H, R, Q, np.zeros(4), np.zeros(2), T, 30_000 + i)[1]
+                         for i in range(B)])
+    offsets = np.arange(B + 1, dtype=np.int64) * T
+    Lq, Lr = np.linalg.cholesky(Q), np.linalg.cholesky(R)
+    tm = S.FunctionalModel(S.models.LinearModel(F), S.MVNSqrt(torch.zeros(4, dtype=torch.float64), torch.as_tensor(Lq)))
+    om = S.FunctionalModel(S.models.LinearModel(H), S.MVNSqrt(torch.zeros(2, dtype=torch.float64), torch.as_tensor(Lr)))
+    x0 = S.MVNSqrt(torch.zeros(4, dtype=torch.float64), torch.eye(4, dtype=torch.float64))
+    ys32 = torch.as_tensor(ys, dtype=torch.float32)
+
+    def reverse():
+        _, adj = S.filter_loglikelihood_adjoint(ys32, x0, tm, om, S.linearization.extended, None, offsets=offsets,
+                                                model_params=False)
+        return np.concatenate([adj["trans_matrix"].sum(0).cpu().numpy().ravel(),
+                               adj["trans_noise_chol"].sum(0).cpu().numpy().ravel()])
+
+    units = []
+    for k in range(16):
+        e = torch.zeros(16, dtype=torch.float64)
+        e[k] = 1.0
+        units.append(e.reshape(4, 4))
+    dirs = [(S.ModelTangent(matrix=u), S.ModelTangent()) for u in units] + \
+           [(S.ModelTangent(noise_chol=u), S.ModelTangent()) for u in units]
+
+    def tangent():
+        g = []
+        for k in range(0, 32, 4):
+            _, gk = S.filter_loglikelihood_grad(ys32, x0, tm, om, S.linearization.extended, None, dirs[k:k + 4],
+                                                offsets=offsets)
+            g.append(gk.sum(0).cpu().numpy())
+        return np.concatenate(g)
+
+    ms_rev, g_rev = _timed(torch, flush, reverse)
+    ms_tan, g_tan = _timed(torch, flush, tangent)
+    scale = np.maximum(1.0, np.abs(g_tan))
+    return {"workload": f"constant velocity nx=4 ny=2, B={B}, T={T}, FP32, d ell / d (F, L_Q): 32 parameters",
+            "reverse_ms": ms_rev, "tangent_ms": ms_tan, "tangent_passes": 8,
+            "max_rel_diff_reverse_vs_tangent": float(np.max(np.abs(g_rev - g_tan) / scale))}
 
 
 def rank_batch(S, batch_size, rank):

@@ -247,6 +247,48 @@ int ss_iterated_grad(const ss_problem* p, const ss_tangents* tangents, const voi
                      int32_t n_iter, double* out_ell, double* out_grad, void* workspace,
                      size_t workspace_bytes, ss_stream_t stream);
 
+/* Reverse-mode gradient of the pseudo-log-likelihood.
+ * Replaces jax.grad of the reference's parallel filter log-likelihood
+ * (parsmooth/parallel/_filtering.py:13-61 with return_loglikelihood, summed
+ * over :149-154) at a fixed nominal trajectory: the gradient of each
+ * sequence's ell with respect to every input array at once, at a cost that
+ * does not grow with the number of parameters.  The filter runs forward and
+ * the smoother's backward associative scan once; the gradient follows from
+ * the smoothed moments of the linearised model (Fisher's identity, exact for
+ * the linear-Gaussian model the filter runs), contracted per step and summed
+ * in FP64.  Every output pointer is a device double array or NULL (not
+ * computed):
+ *   trans_matrix (B, nx, nx), obs_matrix (B, ny, nx): d ell_i / d A of linear
+ *     models (left untouched for other kinds);
+ *   trans_noise_mean (B, nx), obs_noise_mean (B, ny);
+ *   trans_noise_chol (B, nx, nx), obs_noise_chol (B, ny, ny): lower triangles
+ *     (the library reads only those entries), zero above;
+ *   trans_params (B, 4), obs_params (B, 4): d ell_i / d ss_model.params
+ *     (coordinated-turn dt, bearings sensor coordinates, Ricker a), chained
+ *     through each step's linearisation; not with Gauss-Hermite;
+ *   m0 (B, nx), L0 (B, nx, nx) (lower): the prior; with a shared prior
+ *     (prior_per_sequence = 0) row i is sequence i's share, sum the rows.
+ * Built for every (nx, ny) of ss_filter; conditional-moments observation
+ * models (SS_MODEL_POISSON_EXP) and the covariance form are not supported. */
+typedef struct ss_adjoints {
+  double* trans_matrix;
+  double* trans_noise_mean;
+  double* trans_noise_chol;
+  double* obs_matrix;
+  double* obs_noise_mean;
+  double* obs_noise_chol;
+  double* trans_params;
+  double* obs_params;
+  double* m0;
+  double* L0;
+} ss_adjoints;
+
+int ss_filter_adjoint_workspace_bytes(const ss_problem* p, size_t* bytes);
+int ss_filter_adjoint(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+                      int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
+                      double* out_ell, const ss_adjoints* out, void* workspace, size_t workspace_bytes,
+                      ss_stream_t stream);
+
 /* Instrumentation (no counterpart in the reference, which has no tracing):
  * a counter of kernels launched by this library, and per-kernel CUDA-event
  * timing.  While profiling is enabled every launch is bracketed by two events

@@ -11,11 +11,12 @@ __version__ = "1.0.0"
 from ._base import MVNSqrt, MVNStandard, FunctionalModel, ConditionalMomentsModel
 from .methods import (filtering, smoothing, filter_smoother, iterated_smoothing, linearize, FixedIterations,
                       MeanSquaredChange, IteratedSmootherPlan, ModelTangent, filter_loglikelihood_grad,
-                      BearingsLogLikelihood, set_large_state_options, sampling)
+                      BearingsLogLikelihood, set_large_state_options, sampling, filter_loglikelihood_adjoint,
+                      LinearGaussianLogLikelihood)
 from . import linearization, models, data
 
 __all__ = ["MVNSqrt", "MVNStandard", "FunctionalModel", "ConditionalMomentsModel", "filtering", "smoothing",
            "filter_smoother", "iterated_smoothing", "linearize", "FixedIterations", "MeanSquaredChange",
            "IteratedSmootherPlan", "ModelTangent", "filter_loglikelihood_grad", "BearingsLogLikelihood",
-           "set_large_state_options", "sampling",
+           "set_large_state_options", "sampling", "filter_loglikelihood_adjoint", "LinearGaussianLogLikelihood",
            "linearization", "models", "data"]

@@ -20,7 +20,8 @@ SS_OPT_COVARIANCE_FORM = 2
 
 EXPORTED = ("ss_version", "ss_status_string", "ss_supported", "ss_workspace_bytes", "ss_linearize",
             "ss_filter", "ss_smooth", "ss_iterated", "ss_filter_grad", "ss_filter_grad_workspace_bytes",
-            "ss_iterated_grad", "ss_iterated_grad_workspace_bytes", "ss_sample", "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
+            "ss_iterated_grad", "ss_iterated_grad_workspace_bytes", "ss_sample", "ss_filter_adjoint",
+            "ss_filter_adjoint_workspace_bytes", "ss_launch_count", "ss_profile_enable", "ss_profile_read", "ss_profile_reset")
 
 
 class SSModel(ctypes.Structure):
@@ -46,6 +47,12 @@ class SSTangents(ctypes.Structure):
                 ("trans_matrix", ctypes.c_void_p), ("obs_matrix", ctypes.c_void_p),
                 ("trans_noise_mean", ctypes.c_void_p), ("trans_noise_chol", ctypes.c_void_p),
                 ("obs_noise_mean", ctypes.c_void_p), ("obs_noise_chol", ctypes.c_void_p)]
+
+
+class SSAdjoints(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("trans_matrix", "trans_noise_mean", "trans_noise_chol", "obs_matrix", "obs_noise_mean",
+                 "obs_noise_chol", "trans_params", "obs_params", "m0", "L0")]
 
 
 _lock = threading.Lock()
@@ -83,6 +90,9 @@ def load():
         lib.ss_iterated_grad_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
         lib.ss_iterated_grad.argtypes = [PP, ctypes.POINTER(SSTangents), P, P, P, ctypes.c_int32, P, P,
                                          ctypes.c_int32, P, P, P, ctypes.c_size_t, P]
+        lib.ss_filter_adjoint_workspace_bytes.argtypes = [PP, ctypes.POINTER(ctypes.c_size_t)]
+        lib.ss_filter_adjoint.argtypes = [PP, P, P, P, ctypes.c_int32, P, P, P, ctypes.POINTER(SSAdjoints), P,
+                                          ctypes.c_size_t, P]
         lib.ss_sample.argtypes = [PP, P, P, P, P, ctypes.c_int32, P, P, P, ctypes.c_size_t, P]
         lib.ss_profile_enable.argtypes = [ctypes.c_int]
         lib.ss_profile_read.argtypes = [ctypes.c_char_p, ctypes.c_size_t]

@@ -1,0 +1,6 @@
+// Reverse-mode gradient instantiations for dtype f32, nx = 3, ny = 1..3.
+#include "ss_adjoint.cuh"
+
+SS_INST_ADJ(float, f32, 3, 1)
+SS_INST_ADJ(float, f32, 3, 2)
+SS_INST_ADJ(float, f32, 3, 3)

@@ -1,0 +1,6 @@
+// Reverse-mode gradient instantiations for dtype f32, nx = 4, ny = 1..3.
+#include "ss_adjoint.cuh"
+
+SS_INST_ADJ(float, f32, 4, 1)
+SS_INST_ADJ(float, f32, 4, 2)
+SS_INST_ADJ(float, f32, 4, 3)

@@ -26,6 +26,11 @@ SS_FOR_DIMS(SS_DECL)
 SS_FOR_GRAD_DIMS(SS_DECL)
 #undef SS_DECL
 #define SS_DECL(NX, NY)                      \
+  int adj_f32_##NX##_##NY(const Call& c);    \
+  int adj_f64_##NX##_##NY(const Call& c);
+SS_FOR_ADJ_DIMS(SS_DECL)
+#undef SS_DECL
+#define SS_DECL(NX, NY)                      \
   int dense_f32_##NX##_##NY(const Call& c);  \
   int dense_f64_##NX##_##NY(const Call& c);
 SS_FOR_DENSE_DIMS(SS_DECL)
@@ -35,6 +40,14 @@ static RunFn find_grad(int dtype, int nx, int ny) {
 #define SS_CASE(NX, NY) \
   if (nx == NX && ny == NY) return dtype == SS_F32 ? grad_f32_##NX##_##NY : grad_f64_##NX##_##NY;
   SS_FOR_GRAD_DIMS(SS_CASE)
+#undef SS_CASE
+  return nullptr;
+}
+
+static RunFn find_adj(int dtype, int nx, int ny) {
+#define SS_CASE(NX, NY) \
+  if (nx == NX && ny == NY) return dtype == SS_F32 ? adj_f32_##NX##_##NY : adj_f64_##NX##_##NY;
+  SS_FOR_ADJ_DIMS(SS_CASE)
 #undef SS_CASE
   return nullptr;
 }
@@ -456,6 +469,53 @@ int ss_iterated_grad(const ss_problem* p, const ss_tangents* tangents, const voi
   c.n_iter = n_iter;
   c.out_ell = out_ell;
   c.out_grad = out_grad;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  c.stream = reinterpret_cast<cudaStream_t>(stream);
+  return f(c);
+}
+
+int ss_filter_adjoint_workspace_bytes(const ss_problem* p, size_t* bytes) {
+  if (bytes == nullptr) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  if (p->options & SS_OPT_COVARIANCE_FORM) return SS_ERR_UNSUPPORTED;
+  RunFn f = find_adj(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_WORKSPACE;
+  c.p = p;
+  c.ws_bytes_out = bytes;
+  return f(c);
+}
+
+int ss_filter_adjoint(const ss_problem* p, const void* ys, const void* m0, const void* L0,
+                      int32_t prior_per_sequence, const void* nominal_m, const void* nominal_L,
+                      double* out_ell, const ss_adjoints* out, void* workspace, size_t workspace_bytes,
+                      ss_stream_t stream) {
+  if (p == nullptr || out == nullptr || m0 == nullptr || L0 == nullptr) return SS_ERR_INVALID;
+  if (p->total_steps > 0 && ys == nullptr) return SS_ERR_INVALID;
+  if ((nominal_m == nullptr) != (nominal_L == nullptr)) return SS_ERR_INVALID;
+  int rc = validate(p);
+  if (rc) return rc;
+  if (p->options & SS_OPT_COVARIANCE_FORM) return SS_ERR_UNSUPPORTED;
+  if ((out->trans_params != nullptr || out->obs_params != nullptr) && p->lin_method == SS_LIN_GAUSS_HERMITE)
+    return SS_ERR_UNSUPPORTED;
+  RunFn f = find_adj(p->dtype, p->nx, p->ny);
+  if (f == nullptr) return SS_ERR_UNSUPPORTED;
+  Call c;
+  std::memset(&c, 0, sizeof(c));
+  c.op = OP_ADJOINT;
+  c.p = p;
+  c.ys = ys;
+  c.m0 = m0;
+  c.L0 = L0;
+  c.prior_per_sequence = prior_per_sequence;
+  c.nom_m = nominal_m;
+  c.nom_L = nominal_L;
+  c.out_ell = out_ell;
+  c.adjoints = out;
   c.ws = workspace;
   c.ws_bytes = workspace_bytes;
   c.stream = reinterpret_cast<cudaStream_t>(stream);

@@ -9,6 +9,8 @@
   X(5, 1) X(5, 2) X(5, 3)
 // (nx, ny) pairs with forward-mode gradient kernels (ss_filter_grad).
 #define SS_FOR_GRAD_DIMS(X) X(2, 2) X(5, 2)
+// (nx, ny) pairs with reverse-mode gradient kernels (ss_filter_adjoint): all of them.
+#define SS_FOR_ADJ_DIMS(X) SS_FOR_DIMS(X)
 // (nx, ny) pairs of the large-state (dense, warp-per-item) path for linear models.
 #define SS_FOR_DENSE_DIMS(X) X(8, 4) X(32, 16)
 #define SS_MAX_NX 5

@@ -21,6 +21,11 @@ template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_sin(const Dual<T, NT>& a) { return chain(a, ss_sin(a.v), ss_cos(a.v)); }
 template <typename T, int NT>
 SS_DEV Dual<T, NT> ss_cos(const Dual<T, NT>& a) { return chain(a, ss_cos(a.v), -ss_sin(a.v)); }
+template <typename T, int NT>
+SS_DEV Dual<T, NT> ss_exp(const Dual<T, NT>& a) {
+  const T e = ss_exp(a.v);
+  return chain(a, e, e);
+}
 // sin and cos of one angle with one range reduction.  In FP32 a small angle
 // (|x| <= 1/4, the coordinated turn's omega dt in practice) takes the Taylor
 // polynomials to degree 9 / 8, whose truncation error (below 3e-13) is far

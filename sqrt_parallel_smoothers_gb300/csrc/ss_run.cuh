@@ -9,7 +9,7 @@
 namespace ss {
 
 enum { OP_WORKSPACE = 0, OP_LINEARIZE = 1, OP_FILTER = 2, OP_SMOOTH = 3, OP_ITERATED = 4, OP_SUPPORTED = 5,
-       OP_SAMPLE = 6 };
+       OP_SAMPLE = 6, OP_ADJOINT = 7 };
 
 // One entry-point call, dtype-erased.
 struct Call {
@@ -49,6 +49,7 @@ struct Call {
   const ss_tangents* tangents;  // forward-mode directions of the model scalars (gradient runs)
   int32_t n_samples;            // sampler: draws per sequence
   const void* eps;              // sampler: standard normals (states, n_samples, nx)
+  const ss_adjoints* adjoints;  // reverse-mode gradient outputs (ss_filter_adjoint)
 };
 
 typedef int (*RunFn)(const Call&);

@@ -467,6 +467,47 @@ def _(ys, offsets, m0, L0, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, d
     return ys.new_empty((B,), dtype=torch.float64), ys.new_empty((B, n_dir), dtype=torch.float64)
 
 
+# Outputs of ss_filter_adjoint in ss_adjoints order, with their per-sequence shapes.
+ADJOINT_KEYS = ("trans_matrix", "trans_noise_mean", "trans_noise_chol", "obs_matrix", "obs_noise_mean",
+                "obs_noise_chol", "trans_params", "obs_params", "m0", "L0")
+
+
+def _adjoint_shapes(nx, ny):
+    return ((nx, nx), (nx,), (nx, nx), (ny, nx), (ny,), (ny, ny), (4,), (4,), (nx,), (nx, nx))
+
+
+@torch.library.custom_op("sqrtsmooth::filter_adjoint", mutates_args=())
+def _filter_adjoint_op(ys: torch.Tensor, offsets: torch.Tensor, m0: torch.Tensor, L0: torch.Tensor,
+                       nom_m: Optional[torch.Tensor], nom_L: Optional[torch.Tensor], t_mat: Optional[torch.Tensor],
+                       t_qm: torch.Tensor, t_qL: torch.Tensor, o_mat: Optional[torch.Tensor], o_qm: torch.Tensor,
+                       o_qL: torch.Tensor, icfg: List[int], fcfg: List[float]) -> List[torch.Tensor]:
+    nx, ny, B, per, want_params = icfg[0], icfg[1], icfg[10], icfg[13], icfg[14]
+    dev = ys.device
+    pr = _problem(icfg, fcfg, ys.dtype, offsets, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL)
+    lib = _lib.load()
+    nbytes = _lib.ctypes.c_size_t(0)
+    _lib.check(lib.ss_filter_adjoint_workspace_bytes(_lib.ctypes.byref(pr), _lib.ctypes.byref(nbytes)))
+    ws = _workspace(nbytes.value, dev)
+    ell = torch.empty((B,), dtype=torch.float64, device=dev)
+    outs = [torch.zeros((B,) + s, dtype=torch.float64, device=dev) for s in _adjoint_shapes(nx, ny)]
+    adj = _lib.SSAdjoints()
+    for key, t in zip(ADJOINT_KEYS, outs):
+        if key in ("trans_params", "obs_params") and not want_params:
+            continue
+        setattr(adj, key, _ptr(t))
+    _lib.check(lib.ss_filter_adjoint(_lib.ctypes.byref(pr), _ptr(ys), _ptr(m0), _ptr(L0), per, _ptr(nom_m),
+                                     _ptr(nom_L), _ptr(ell), _lib.ctypes.byref(adj), _ptr(ws), nbytes.value,
+                                     _stream(dev)))
+    return [ell] + outs
+
+
+@_filter_adjoint_op.register_fake
+def _(ys, offsets, m0, L0, nom_m, nom_L, t_mat, t_qm, t_qL, o_mat, o_qm, o_qL, icfg, fcfg):
+    nx, ny, B = icfg[0], icfg[1], icfg[10]
+    return [ys.new_empty((B,), dtype=torch.float64)] + \
+        [ys.new_empty((B,) + s, dtype=torch.float64) for s in _adjoint_shapes(nx, ny)]
+
+
 # ----------------------------------------------------------------------------- public API
 
 def _factor(P):
@@ -1311,10 +1352,12 @@ class BearingsLogLikelihood(torch.autograd.Function):
     vector-Jacobian product.  ``ell`` is summed over the batch.  With ``n_iter > 0`` the
     log-likelihood is the iterated smoother's after ``n_iter`` calls from ``nominal`` (the
     pseudo-log-likelihood of the reference's parameter estimation), differentiated through
-    the iterations."""
+    the iterations.  ``mode="reverse"`` (``n_iter = 0`` only) takes the gradient from one
+    reverse pass instead (:func:`filter_loglikelihood_adjoint`)."""
 
     @staticmethod
-    def forward(ctx, theta, observations, x0, nominal, Q1, dt, s2, method, lengths, offsets, n_iter=0):
+    def forward(ctx, theta, observations, x0, nominal, Q1, dt, s2, method, lengths, offsets, n_iter=0,
+                mode="tangent"):
         from .models import Bearings, CoordinatedTurn
         th = theta.detach().double().cpu()
         s1 = (float(th[0]), float(th[1]))
@@ -1323,16 +1366,108 @@ class BearingsLogLikelihood(torch.autograd.Function):
         cR = sigma * torch.eye(2, dtype=torch.float64)
         tm = FunctionalModel(CoordinatedTurn(dt), MVNSqrt(torch.zeros(5, dtype=torch.float64), cQ))
         om = FunctionalModel(Bearings(s1, s2), MVNSqrt(torch.zeros(2, dtype=torch.float64), cR))
-        dirs = [(ModelTangent(), ModelTangent(params=[1, 0, 0, 0])),
-                (ModelTangent(), ModelTangent(params=[0, 1, 0, 0])),
-                (ModelTangent(noise_chol=0.5 * cQ), ModelTangent()),
-                (ModelTangent(), ModelTangent(noise_chol=cR))]
-        ell, grad = filter_loglikelihood_grad(observations, x0, tm, om, method, nominal, dirs, lengths=lengths,
-                                              offsets=offsets, n_iter=n_iter)
-        ctx.save_for_backward(grad.reshape(-1, 4).sum(0).to(device=theta.device, dtype=theta.dtype))
+        if mode == "reverse":
+            if n_iter:
+                raise ValueError("the reverse pass differentiates the filter at a fixed nominal (n_iter = 0)")
+            ell, adj = filter_loglikelihood_adjoint(observations, x0, tm, om, method, nominal, lengths=lengths,
+                                                    offsets=offsets)
+            dev = adj["obs_params"].device
+            op = adj["obs_params"].reshape(-1, 4).sum(0)
+            gq = (adj["trans_noise_chol"].reshape(-1, 5, 5).sum(0) * (0.5 * cQ).to(dev)).sum()
+            gr = (adj["obs_noise_chol"].reshape(-1, 2, 2).sum(0) * cR.to(dev)).sum()
+            grad = torch.stack([op[0], op[1], gq, gr])
+        elif mode == "tangent":
+            dirs = [(ModelTangent(), ModelTangent(params=[1, 0, 0, 0])),
+                    (ModelTangent(), ModelTangent(params=[0, 1, 0, 0])),
+                    (ModelTangent(noise_chol=0.5 * cQ), ModelTangent()),
+                    (ModelTangent(), ModelTangent(noise_chol=cR))]
+            ell, grad = filter_loglikelihood_grad(observations, x0, tm, om, method, nominal, dirs, lengths=lengths,
+                                                  offsets=offsets, n_iter=n_iter)
+            grad = grad.reshape(-1, 4).sum(0)
+        else:
+            raise ValueError(f"mode must be 'tangent' or 'reverse', got {mode!r}")
+        ctx.save_for_backward(grad.to(device=theta.device, dtype=theta.dtype))
         return ell.sum().to(device=theta.device, dtype=theta.dtype)
 
     @staticmethod
     def backward(ctx, grad_out):
         (g,) = ctx.saved_tensors
-        return (grad_out * g.to(grad_out.device),) + (None,) * 10
+        return (grad_out * g.to(grad_out.device),) + (None,) * 11
+
+
+def filter_loglikelihood_adjoint(observations, x0, transition_model, observation_model, linearization_method,
+                                 nominal_trajectory=None, *, lengths=None, offsets=None, chunk=0, group=0,
+                                 slr_form=0, model_params=None):
+    """Log-likelihood of the parallel filter and its gradient with respect to every input, from
+    one reverse pass (``ss_filter_adjoint``).
+
+    The reference obtains these by ``jax.grad`` through its parallel filter
+    (parsmooth/parallel/_filtering.py:13-61 with ``return_loglikelihood``).  Here the filter and
+    the smoother's backward scan run once at the given nominal, and the gradient comes from the
+    smoothed moments of the linearised model (Fisher's identity), so the cost does not depend
+    on how many parameters are differentiated.  Returns ``(ell, adj)``: ``adj`` maps each of
+    ``ADJOINT_KEYS`` to ``d ell / d (that input)`` in FP64, per sequence for batches:
+    ``trans_matrix`` / ``obs_matrix`` (linear models), the noise means, the noise square roots
+    (lower triangles, as the library reads them), ``trans_params`` / ``obs_params`` (the device
+    models' scalars: coordinated-turn ``dt``, bearings sensor coordinates, Ricker ``a``), and the
+    prior's ``m0`` / ``L0`` (with a shared prior each sequence's share).  ``model_params``:
+    compute the model-scalar gradients (default: unless the method is Gauss-Hermite, which the
+    dual-number chain does not cover)."""
+    method = _check_common(x0, True, linearization_method)
+    if nominal_trajectory is not None:
+        are_inputs_compatible(x0, nominal_trajectory)
+    if model_params is None:
+        model_params = method.code != _lib.SS_LIN_GAUSS_HERMITE
+    dev = _device()
+    lay = _Layout(observations, lengths, offsets, None, dev)
+    nx = int(torch.as_tensor(x0.mean).shape[-1])
+    fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
+    fn_o, o_mat, o_qm, o_qL = _model_tensors(observation_model, nx, lay.ny, lay.dtype, dev)
+    m0, L0, per = _prior(x0, lay, nx)
+    nm, nL = _nominal(nominal_trajectory, lay, nx)
+    icfg = _icfg(method, nx, lay.ny, fn_t, fn_o, lay, chunk, group, slr_form, [per, int(bool(model_params))])
+    res = torch.ops.sqrtsmooth.filter_adjoint(lay.ys, lay.offsets, m0, L0, nm, nL, t_mat, t_qm, t_qL, o_mat, o_qm,
+                                              o_qL, icfg, _fcfg(method, fn_t, fn_o))
+    adj = {k: lay.per_sequence(v) for k, v in zip(ADJOINT_KEYS, res[1:])}
+    if not model_params:
+        del adj["trans_params"], adj["obs_params"]
+    return lay.per_sequence(res[0]), adj
+
+
+class LinearGaussianLogLikelihood(torch.autograd.Function):
+    """Log-likelihood of the parallel square-root filter for a linear-Gaussian model,
+    ``ell(F, L_Q, b, H, L_R, c, m0, L0)`` summed over the batch, differentiable in all eight
+    arrays at once: the forward pass runs :func:`filter_loglikelihood_adjoint` (one filter,
+    one smoother scan, one contraction) and backward scales the stored gradients.
+
+    ``x_t = F x_{t-1} + b + N(0, L_Q L_Q^T)``, ``y_t = H x_t + c + N(0, L_R L_R^T)``,
+    ``x_0 ~ N(m0, L0 L0^T)`` (``m0`` (nx,) shared or (B, nx) per sequence); the square roots are
+    read as lower triangles.  ``observations``, ``lengths``, ``offsets`` as in
+    :func:`filtering`."""
+
+    @staticmethod
+    def forward(ctx, F, Lq, b, H, Lr, c, m0, L0, observations, lengths=None, offsets=None):
+        from .models import LinearModel
+        from .linearization import extended
+        d = lambda t: t.detach()
+        tm = FunctionalModel(LinearModel(d(F)), MVNSqrt(d(b), d(Lq)))
+        om = FunctionalModel(LinearModel(d(H)), MVNSqrt(d(c), d(Lr)))
+        ell, adj = filter_loglikelihood_adjoint(observations, MVNSqrt(d(m0), d(L0)), tm, om, extended, None,
+                                                lengths=lengths, offsets=offsets, model_params=False)
+        batched = ell.ndim == 1
+
+        def total(key, like):
+            g = adj[key]
+            if batched and g.ndim == like.ndim + 1:
+                g = g.sum(0)
+            return g.to(device=like.device, dtype=like.dtype).reshape(like.shape)
+
+        grads = [total("trans_matrix", F), total("trans_noise_chol", Lq), total("trans_noise_mean", b),
+                 total("obs_matrix", H), total("obs_noise_chol", Lr), total("obs_noise_mean", c),
+                 total("m0", m0), total("L0", L0)]
+        ctx.save_for_backward(*grads)
+        return ell.sum().to(device=F.device, dtype=F.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        return tuple(grad_out.to(g.device) * g for g in ctx.saved_tensors) + (None,) * 3
