@@ -51,6 +51,15 @@ def _compile(src, obj, verbose):
     return r.stderr
 
 
+def _weight(src):
+    """Rough compile cost of an instantiation unit: dual-number units, FP64 and larger state
+    sizes take longest."""
+    name = os.path.basename(src)
+    nums = [int(t) for t in name[:-3].split("_") if t.isdigit()]
+    nx = nums[0] if nums else 0
+    return 4 * ("grad" in name) + 2 * ("f64" in name) + ("adj" in name) + nx / 4
+
+
 def build(verbose=False, jobs=None):
     """Compile and link the library; return its path."""
     os.makedirs(BUILD, exist_ok=True)
@@ -66,7 +75,7 @@ def build(verbose=False, jobs=None):
     jobs = jobs or max(1, min(len(todo), os.cpu_count() or 1))
     if todo:
         # the largest units first so the tail of the parallel build is short
-        todo.sort(key=lambda so: ("grad" not in so[0], "f64" not in so[0], "_5_" not in so[0]))
+        todo.sort(key=lambda so: -_weight(so[0]))
         with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
             for log in ex.map(lambda so: _compile(so[0], so[1], verbose), todo):
                 if verbose and log:

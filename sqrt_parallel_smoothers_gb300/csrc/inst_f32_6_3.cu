@@ -1,0 +1,4 @@
+// Kernel instantiations for dtype f32, (nx, ny) = (6, 3).
+#include "ss_run.cuh"
+
+SS_INST(float, f32, 6, 3)

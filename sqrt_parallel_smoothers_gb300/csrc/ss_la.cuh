@@ -324,6 +324,12 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
 template <typename R, int ROWS, int COLS, class PAT, bool GUARD = false>
 SS_DEV void tria_sp(R (&M)[ROWS][COLS]) {
   static_assert(COLS >= ROWS, "tria expects at least as many columns as rows");
+  if constexpr (COLS > 64) {
+    // wider than a 64-bit pattern mask (sigma-point regressions of conditional models at
+    // nx >= 8): the unpatterned triangularisation
+    tria<R, ROWS, COLS, GUARD>(M);
+    return;
+  }
   // entries outside the pattern are zero: say so, so that they cost no registers
   SS_UNROLL
   for (int r = 0; r < ROWS; ++r) {

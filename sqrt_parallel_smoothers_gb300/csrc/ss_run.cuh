@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "ss_dims.h"
 #include "ss_staged.cuh"
 
 namespace ss {
@@ -210,11 +211,19 @@ constexpr int LEVEL_BLOCK = 32;
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block > 0 ? (n + block - 1) / block : 1); }
 
+// The shared-memory staged kernels (ss_staged.cuh) serve types with a 16-byte
+// vector form whose staging tiles fit a block; the others take the plain kernels.
+template <typename R, int NX, int NY>
+constexpr bool use_staged() {
+  if constexpr (Vec16<R>::vec) return StagedSmem<R, NX, NY>::fits;
+  else return false;
+}
+
 // Lin-kernel dispatch over the model pair and method.
 template <typename R, int NX, int NY, class TF, class OF, int METHOD>
 inline int launch_lin_one(const LinArgs<R>& a, cudaStream_t st) {
   const unsigned grid = grid_for(a.total, STAGED_BLOCK);
-  if constexpr (Vec16<R>::vec) {
+  if constexpr (use_staged<R, NX, NY>()) {
     constexpr int sm = (int)StagedSmem<R, NX, NY>::lin;
     cudaFuncSetAttribute(lin_staged_kernel<R, NX, NY, TF, OF, METHOD>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     SS_LAUNCH("lin", st, launch_pdl(lin_staged_kernel<R, NX, NY, TF, OF, METHOD>, grid, STAGED_BLOCK, sm, st, a));
@@ -399,7 +408,7 @@ struct Runner {
 
   int filter_pass(bool emit_smoother) {
     const unsigned g1 = grid_for(y.items[1], STAGED_BLOCK);
-    if constexpr (Vec16<R>::vec) {
+    if constexpr (use_staged<R, NX, NY>()) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::leaf;
       cudaFuncSetAttribute(filter_leaf_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       SS_LAUNCH("filter_leaf", st, launch_pdl(filter_leaf_staged_kernel<R, NX, NY>, g1, STAGED_BLOCK, sm, st, sa));
@@ -409,7 +418,7 @@ struct Runner {
     int rc = filter_scan();
     if (rc) return rc;
     sa.emit_smoother = emit_smoother ? 1 : 0;
-    if constexpr (Vec16<R>::vec) {
+    if constexpr (use_staged<R, NX, NY>()) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::fwalk;
       cudaFuncSetAttribute(filter_walk_staged_kernel<R, NX, NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       SS_LAUNCH("filter_walk", st, launch_pdl(filter_walk_staged_kernel<R, NX, NY>, g1, STAGED_BLOCK, sm, st, sa));
@@ -427,7 +436,7 @@ struct Runner {
     for (int l = y.L - 1; l >= 1; --l) {
       SS_LAUNCH("smoother_down", st, launch_pdl(smoother_down_kernel<R, NX>, grid_for(y.items[l + 1], LEVEL_BLOCK), LEVEL_BLOCK, 0, st, sa, l));
     }
-    if constexpr (Vec16<R>::vec) {
+    if constexpr (use_staged<R, NX, NY>()) {
       constexpr int sm = (int)StagedSmem<R, NX, NY>::swalk;
       cudaFuncSetAttribute(smoother_walk_staged_kernel<R, NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
       SS_LAUNCH("smoother_walk", st,
@@ -528,7 +537,7 @@ struct Runner {
     // pieces, 80 bytes for nx = 5) in the factor buffers; only the caller's
     // initial nominal and the final output use the caller's layout.  The
     // dual-number kernels keep the caller's layout throughout.
-    constexpr bool packed = Vec16<R>::vec;
+    constexpr bool packed = use_staged<R, NX, NY>();
     const R* cur_m = static_cast<const R*>(c.nom_m);
     const R* cur_L = static_cast<const R*>(c.nom_L);
     const R* cur_rec = nullptr;
@@ -642,7 +651,7 @@ int run(const Call& c) {
     return models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind) ? SS_OK : SS_ERR_UNSUPPORTED;
   if (!models_supported<R, NX, NY>(c.p->transition.kind, c.p->observation.kind)) return SS_ERR_UNSUPPORTED;
   if (c.p->options & SS_OPT_COVARIANCE_FORM) {
-    if constexpr (Tangents<R>::n == 0) return run_std<R, NX, NY>(c);
+    if constexpr (Tangents<R>::n == 0 && NX <= SS_MAX_NX && NY <= SS_MAX_NY) return run_std<R, NX, NY>(c);
     else return SS_ERR_UNSUPPORTED;
   }
   if (c.op == OP_WORKSPACE) {

@@ -83,6 +83,9 @@ struct StagedSmem {
                                                                                   : StageTile<R, Q::ST>::STRIDE;
   static constexpr size_t swalk = sizeof(R) * STAGED_WARPS *
                                   (2 * StageTile<R, Q::SE>::WARP_ELEMS + 32 * out_stride);
+  // every staged kernel's tiles fit one block's 227 KB (not FP64 at nx >= 6, whose records
+  // run through the unstaged kernels)
+  static constexpr bool fits = lin <= 232448 && leaf <= 232448 && fwalk <= 232448 && swalk <= 232448;
 };
 
 template <typename R>

@@ -629,10 +629,12 @@ def _dummy_observation(nx, dtype, device, ny=1):
         torch.eye(ny, dtype=dtype, device=device)
 
 
-def _dummy_ny(nx):
-    """Observation size of the placeholder model when a transition is linearised alone: the
-    compiled large-state (nx > 5) kernels pair nx with ny = nx / 2."""
-    return 1 if nx <= 5 else nx // 2
+def _dummy_ny(nx, fn=None):
+    """Observation size of the placeholder model when a transition is linearised alone: 1,
+    except for linear transitions at the large-state sizes, whose compiled kernels pair nx with
+    ny = nx / 2."""
+    linear = fn is None or getattr(fn, "kind", None) == _lib.SS_MODEL_LINEAR
+    return nx // 2 if (linear and nx in (8, 32)) else 1
 
 
 def filtering(observations, x0, transition_model, observation_model, linearization_method,
@@ -725,7 +727,7 @@ def _smoothing_std(transition_model, filter_trajectory, linearization_method, no
     dtype = fm.dtype if fm.dtype in _DT else torch.float32
     lay = _smooth_layout(fm, lengths, offsets, dtype, dev)
     fn_t, t_mat, t_qm, t_Q = _model_tensors_std(transition_model, nx, nx, lay.dtype, dev)
-    ny = _dummy_ny(nx)
+    ny = _dummy_ny(nx, fn_t)
     fn_o, o_mat, o_qm, o_Q = _dummy_observation(nx, lay.dtype, dev, ny)
     fmp = lay.pack_states(filter_trajectory.mean, (nx,))
     fPp = lay.pack_states(filter_trajectory.cov, (nx, nx)).contiguous()
@@ -775,7 +777,7 @@ def smoothing(transition_model, filter_trajectory, linearization_method, nominal
         B, Tp1 = fm.shape[:2]
         lay = _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
     fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
-    ny = _dummy_ny(nx)
+    ny = _dummy_ny(nx, fn_t)
     fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev, ny)
     fmp = lay.pack_states(filter_trajectory.mean, (nx,))
     fLp = _lower_batched(lay.pack_states(filter_trajectory.chol, (nx, nx)))
@@ -825,7 +827,7 @@ def sampling(key, n_samples, transition_model, filter_trajectory, linearization_
         B, Tp1 = fm.shape[:2]
         lay = _Layout(torch.zeros((B, Tp1 - 1, 1), dtype=dtype), lengths, None, dtype, dev)
     fn_t, t_mat, t_qm, t_qL = _model_tensors(transition_model, nx, nx, lay.dtype, dev)
-    ny = _dummy_ny(nx)
+    ny = _dummy_ny(nx, fn_t)
     fn_o, o_mat, o_qm, o_qL = _dummy_observation(nx, lay.dtype, dev, ny)
     fmp = lay.pack_states(filter_trajectory.mean, (nx,))
     fLp = _lower_batched(lay.pack_states(filter_trajectory.chol, (nx, nx)))
@@ -976,7 +978,7 @@ def linearize(model, x, method, *, covariance_form="operators"):
         ny = d_out
     else:
         fn_t, t_mat, t_qm, t_qL = fnm, mat, qm, qL
-        ny = _dummy_ny(nx)
+        ny = _dummy_ny(nx, fnm)
         o = _dummy_observation(nx, dtype, dev, ny)
     lay_off = torch.zeros(2, dtype=torch.int64, device=dev)
 
@@ -1016,7 +1018,7 @@ def _linearize_std(model, x, method):
         ny = d_out
     else:
         fn_t, t_mat, t_qm, t_Q = fnm, mat, qm, Q
-        ny = _dummy_ny(nx)
+        ny = _dummy_ny(nx, fnm)
         o = _dummy_observation(nx, dtype, dev, ny)
     lay_off = torch.zeros(2, dtype=torch.int64, device=dev)
 

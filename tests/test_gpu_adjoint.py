@@ -3,7 +3,10 @@ the oracle's restatement (smoothed moments contracted per step, FP64; itself che
 central differences of the oracle's log-likelihood in test_oracle_adjoint.py), against the
 tangent-linear path, and through the torch.autograd.Function interfaces.
 
-Tolerances: FP64 1e-9 relative to the largest entry (the same arithmetic in another order);
+Tolerances: FP64 1e-9 relative to the largest entry (the same arithmetic in another order),
+widened to 4 cond(c)^2 eps where a random noise or prior factor c is ill-conditioned (every
+contraction solves with c twice), and 1e-8 on the bearings model (its process noise factor has
+entries of 1e-4, so rounding differences of the two linearisations are amplified by Q^-1);
 FP32 5e-3 on short sequences and 1e-2 on the config of the reference's parameter-estimation
 study at B = 64, T = 5000, against FP64 finite differences."""
 import numpy as np
@@ -39,9 +42,11 @@ def test_linear_adjoints_fp64_vs_oracle(nx, ny):
     x0 = S.MVNSqrt(torch.as_tensor(x0o.mean), torch.as_tensor(x0o.chol))
     ell, got = S.filter_loglikelihood_adjoint(torch.as_tensor(ys), x0, gt, go, S.linearization.extended)
     assert abs(float(ell) - ell_ref) <= 1e-10 * max(1.0, abs(ell_ref))
+    cond = max(np.linalg.cond(c) for c in (s["cholQ"], s["cholR"], s["chol_x0"].chol))
+    tol = max(1e-9, 4 * cond ** 2 * np.finfo(float).eps)
     for key in ("trans_matrix", "trans_noise_mean", "trans_noise_chol", "obs_matrix", "obs_noise_mean",
                 "obs_noise_chol", "m0", "L0"):
-        assert_rel(got[key], ref[key], 1e-9, key)
+        assert_rel(got[key], ref[key], tol, key)
     assert np.all(np_(got["trans_params"]) == 0) and np.all(np_(got["obs_params"]) == 0)
 
 
@@ -144,16 +149,16 @@ def test_bearings_model_params_fp64_vs_oracle(method):
     assert abs(float(ell) - ell_ref) <= 1e-10 * abs(ell_ref)
     # the oracle's parameter chain differentiates the local linearisation numerically (h = 1e-6)
     assert_rel(got["obs_params"], np.array(ref_params), 1e-6, "obs_params")
-    assert_rel(got["trans_noise_chol"], OA.noise_chol_adjoint(adj["A_q"], adj["lin"][1], tm.mvn.chol), 1e-9,
+    assert_rel(got["trans_noise_chol"], OA.noise_chol_adjoint(adj["A_q"], adj["lin"][1], tm.mvn.chol), 1e-8,
                "trans_noise_chol")
-    assert_rel(got["obs_noise_chol"], OA.noise_chol_adjoint(adj["A_r"], adj["lin"][4], om.mvn.chol), 1e-9,
+    assert_rel(got["obs_noise_chol"], OA.noise_chol_adjoint(adj["A_r"], adj["lin"][4], om.mvn.chol), 1e-8,
                "obs_noise_chol")
-    assert_rel(got["trans_noise_mean"], adj["b"].sum(0), 1e-9, "trans_noise_mean")
-    assert_rel(got["m0"], adj["m0"], 1e-9, "m0")
+    assert_rel(got["trans_noise_mean"], adj["b"].sum(0), 1e-8, "trans_noise_mean")
+    assert_rel(got["m0"], adj["m0"], 1e-8, "m0")
 
 
-@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-8), (torch.float32, 5e-3)])
-def test_reverse_matches_tangent_path_bearings(dtype, tol):
+@pytest.mark.parametrize("dtype,tol,ell_tol", [(torch.float64, 1e-8, 1e-9), (torch.float32, 5e-3, 1e-5)])
+def test_reverse_matches_tangent_path_bearings(dtype, tol, ell_tol):
     """The reverse pass and the tangent-linear pass give the same four derivatives."""
     T = 200
     ys, m0, nom, Q1, theta = _bearings_problem(T, seed=5)
@@ -166,8 +171,9 @@ def test_reverse_matches_tangent_path_bearings(dtype, tol):
         ell = S.BearingsLogLikelihood.apply(t, torch.as_tensor(ys, dtype=dtype), x0, nomg, Q1, 0.01, (1.0, 1.0),
                                             S.linearization.cubature, None, None, 0, mode)
         ell.backward()
-        out[mode] = (float(ell), t.grad.numpy().copy())
-    assert abs(out["tangent"][0] - out["reverse"][0]) <= 1e-9 * abs(out["tangent"][0])
+        out[mode] = (float(ell.detach()), t.grad.numpy().copy())
+    # the FP32 tangent pass runs the dual-number kernels, the reverse pass the primal ones
+    assert abs(out["tangent"][0] - out["reverse"][0]) <= ell_tol * abs(out["tangent"][0])
     g_t, g_r = out["tangent"][1], out["reverse"][1]
     assert np.all(np.abs(g_r - g_t) <= tol * np.maximum(1.0, np.abs(g_t))), (g_r, g_t)
 

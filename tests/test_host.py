@@ -98,6 +98,22 @@ def test_large_state_dims_are_linear_only():
     assert lib.ss_supported(ctypes.byref(p2)) == 0
 
 
+def test_wide_dims_are_supported_and_nine_states_are_not():
+    """ss_supported answers for the six- to eight-state pairs (a nonlinear model included)."""
+    lib = _lib.load()
+    dummy = ctypes.c_double(0)
+    for nx, ny, ok in ((6, 2, 1), (7, 2, 1), (8, 2, 1), (8, 1, 1), (6, 3, 1), (9, 2, 0), (7, 3, 0)):
+        p = _lib.SSProblem()
+        p.dtype, p.nx, p.ny, p.lin_method, p.batch, p.gh_order = _lib.SS_F32, nx, ny, _lib.SS_LIN_CUBATURE, 1, 3
+        p.transition.kind = _lib.SS_MODEL_RICKER
+        p.observation.kind = _lib.SS_MODEL_BEARINGS if ny == 2 else _lib.SS_MODEL_LINEAR
+        for mdl in (p.transition, p.observation):
+            mdl.matrix = mdl.noise_mean = mdl.noise_chol = ctypes.addressof(dummy)
+        p.offsets = ctypes.addressof(dummy)
+        p.total_steps = p.max_len = 10
+        assert lib.ss_supported(ctypes.byref(p)) == ok, (nx, ny)
+
+
 def test_calls_without_workspace_fail_cleanly():
     lib = _lib.load()
     p, keep = _problem()
