@@ -268,8 +268,9 @@ int ss_iterated_grad(const ss_problem* p, const ss_tangents* tangents, const voi
  *     through each step's linearisation; not with Gauss-Hermite;
  *   m0 (B, nx), L0 (B, nx, nx) (lower): the prior; with a shared prior
  *     (prior_per_sequence = 0) row i is sequence i's share, sum the rows.
- * Built for every (nx, ny) of ss_filter; conditional-moments observation
- * models (SS_MODEL_POISSON_EXP) and the covariance form are not supported. */
+ * Built for nx <= 5, ny <= 3; conditional-moments observation models
+ * (SS_MODEL_POISSON_EXP) and the covariance form are not supported.  The
+ * workspace also holds the call's filtered and smoothed trajectories. */
 typedef struct ss_adjoints {
   double* trans_matrix;
   double* trans_noise_mean;

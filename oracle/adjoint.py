@@ -30,7 +30,7 @@ against central differences of the oracle's log-likelihood.
 import numpy as np
 
 from . import parallel as par
-from .core import mT, mv, solve_lower, solve_upper
+from .core import mT, mv, solve_lower, solve_upper, tria
 from .types import MVNSqrt
 
 
@@ -150,3 +150,26 @@ def param_adjoint(adj, which, lin_plus, lin_minus, h):
     # tr(Qbar (dc c^T + c dc^T)) = tr(c^-T A c^-1 dc c^T) = tr(A c^-1 dc)
     X = _whiten(c, dc)
     return float(np.sum(Fbar * dF) + np.sum(bbar * db) + np.einsum("tij,tji->", A, X))
+
+
+def transition_adjoint_predicted_form(F, cQ, b, fm, fL, sm, sL):
+    """The transition part of :func:`filter_adjoint` written with the filter's predicted moments
+    instead of the residual ``e_t`` (the form the GPU kernel computes): with ``Lp`` the predicted
+    factor from ``tria([[F Lf, cQ], [Lf, 0]])`` (whose lower-left block is ``Phi21 = E Lp``),
+    ``d = ms_t - mp_t`` and ``[Y, y] = Lp^-1 [Ls_t, d]``,
+    ``dl/dQ = Lp^-T (Y Y^T - I + y y^T) Lp^-1 / 2``, ``dl/db = Lp^-T y`` and
+    ``dl/dF = Lp^-T ((Y Y^T - I) Phi21^T + y ms_{t-1}^T)``.  ``fm, fL`` / ``sm, sL``: filtered
+    and smoothed trajectories (T + 1 states).  Returns ``(Fbar, bbar, Qbar)`` per step."""
+    nx = cQ.shape[-1]
+    Phi = tria(np.concatenate([np.concatenate([F @ fL[:-1], cQ], -1),
+                               np.concatenate([fL[:-1], np.zeros_like(cQ)], -1)], -2))
+    Lp, P21 = Phi[..., :nx, :nx], Phi[..., nx:, :nx]
+    d = sm[1:] - (mv(F, fm[:-1]) + b)
+    Y = solve_lower(Lp, np.concatenate([sL[1:], d[..., None]], -1))
+    Y1, y = Y[..., :nx], Y[..., nx]
+    Ap = Y1 @ mT(Y1) - np.eye(nx)
+    N = Ap + y[..., None] * y[..., None, :]
+    Fbar = _unwhiten_T(Lp, Ap @ mT(P21) + y[..., None] * sm[:-1][..., None, :])
+    bbar = _unwhiten_T(Lp, y[..., None])[..., 0]
+    Qbar = 0.5 * _unwhiten_T(Lp, mT(_unwhiten_T(Lp, N)))
+    return Fbar, bbar, Qbar

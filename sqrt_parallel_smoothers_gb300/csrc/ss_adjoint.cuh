@@ -10,20 +10,19 @@
 // expectation of the complete-data score (Fisher's identity), which needs only
 // the smoothed moments.  The reverse pass is therefore the smoother's own
 // backward associative scan, run once whatever the number of parameters, plus
-// one per-step contraction:
-//   transition residual e_t = x_t - F x_{t-1} - b, from the smoothing element
-//     x_{t-1} = E x_t + g + D w (the one the filter walk emits) and the smoothed
-//     x_t ~ N(ms_t, Ls_t Ls_t^T): mean ms_t - F ms_{t-1} - b, covariance factor
-//     [(I - F E) Ls_t, F D];
-//   Z = cQ^-1 [(I - F E) Ls_t, F D, E e],   A_q = Z Z^T - I,
-//   dl/dF = cQ^-T (Z_1 (E Ls_t)^T - Z_2 D^T + z_e ms_{t-1}^T),  dl/db = cQ^-T z_e,
-//   dl/dQ = cQ^-T A_q cQ^-1 / 2, so for a factor L of an additive part of Q,
-//   dl/dL = cQ^-T A_q cQ^-1 L;  and the same forms for the observation residual
-//   y_t - H x_t - c (Z_y = cR^-1 [H Ls_t, E r]) and the prior.
-// The whitened form keeps the FP32 cancellation inside the O(1) matrix A.
+// one per-step contraction of the filtered, predicted and smoothed moments:
+//   transition (adjoint_transition): with d = ms_t - mp_t (smoothed minus
+//     predicted mean), [Y, y] = Lp^-1 [Ls_t, d] (Lp the predicted factor) and
+//     N = Y Y^T - I + y y^T:  dl/dQ = Lp^-T N Lp^-1 / 2, dl/db = Lp^-T y,
+//     dl/dF = Lp^-T ((Y Y^T - I) (E Lp)^T + y ms_{t-1}^T); for a factor L of an
+//     additive part of Q, dl/dL = Lp^-T N Lp^-1 L;
+//   observation (adjoint_observation): Z = cR^-1 [H Ls_t, y_t - H ms_t - c],
+//     A = Z Z^T - I: dl/dR = cR^-T A cR^-1 / 2, dl/dH = cR^-T (z_r ms_t^T - Z_1 Ls_t^T),
+//     dl/dc = cR^-T z_r;
+//   prior (adjoint_prior_kernel): the observation's form with L0 and ms_0 - m0.
 // Model parameters that enter a nonlinear model's linearisation are chained
 // per step through a one-direction dual-number linearisation (at most four per
-// model): tr(Fbar^T dF) + bbar . db + tr(A c^-1 dc).
+// model): tr(Fbar^T dF) + bbar . db + tr(Qbar d(c c^T)).
 //
 // Work decomposition: one thread per level-1 chunk (the scan's geometry)
 // accumulates its steps' contributions in FP64 (a per-thread column of shared
@@ -45,86 +44,70 @@ constexpr int ADJ_BLOCK = 64;
 
 template <typename R, int NX, int NY>
 struct AdjTrans {
-  R Fbar[NX][NX], bbar[NX], A[NX][NX];
+  R Fbar[NX][NX], bbar[NX];
+  R N[NX][NX];    // dl/dQ = Lp^-T N Lp^-1 / 2
+  R Lp[NX][NX];   // the filter's predicted factor
 };
 template <typename R, int NX, int NY>
 struct AdjObs {
   R Hbar[NY][NX], cbar[NY], A[NY][NY];
 };
 
-// Transition part of step t: l = the step's linearisation, se = the smoothing
-// element of x_{t-1}, mp = ms_{t-1}, sn = smoothed x_t.
+// Transition part of step t (x_{t-1} -> x_t), in the predicted-moment
+// (disturbance-smoother) form.  With the filter's predicted moments of x_t
+// (mean mp = F mf + b; factor Lp from tria([[F Lf, cQ], [Lf, 0]]), whose
+// lower-left block is Phi21 = E Lp for the smoothing gain E) and the smoothed
+// x_t ~ N(ms, Ls Ls^T), the residual e = x_t - F x_{t-1} - b has E e = Q P^-1 d
+// and Q^-1 Cov(e) Q^-1 - Q^-1 = P^-1 (Ps - P) P^-1, d = ms - mp.  So with
+// [Y, y] = Lp^-1 [Ls, d] and N = Y Y^T - I + y y^T:
+//   dl/dQ = Lp^-T N Lp^-1 / 2,   dl/db = Lp^-T y,
+//   dl/dF = Lp^-T ((Y Y^T - I) Phi21^T + y ms_{t-1}^T).
+// Nothing subtracts two states to form the O(sqrt Q) residual itself: FP32
+// smoothed means carry errors far above sqrt Q when the process noise is small
+// against the state, and Q^-1 would amplify them.  f = filtered x_{t-1},
+// msp = smoothed mean of x_{t-1}, sn = smoothed x_t.
 template <typename R, int NX, int NY>
-SS_DEV void adjoint_transition(const Lin<R, NX, NY>& l, const SElem<R, NX>& se, const R (&mp)[NX],
+SS_DEV void adjoint_transition(const Lin<R, NX, NY>& l, const State<R, NX>& f, const R (&msp)[NX],
                                const State<R, NX>& sn, AdjTrans<R, NX, NY>& o) {
-  constexpr int WC = 2 * NX + 1;
-  R M[NX][NX];   // I - F E
+  R X[2 * NX][2 * NX], mp[NX];
+  SElem<R, NX> se;
+  smoother_element<R, NX>(l.F, l.cQ, l.bq, f, se, X, mp);
+  R Y[NX][NX + 1];
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
-    for (int j = 0; j < NX; ++j) {
-      R q = (i == j) ? R(1) : R(0);
-      SS_UNROLL
-      for (int k = 0; k < NX; ++k) q -= l.F[i][k] * se.E[k][j];
-      M[i][j] = q;
-    }
+    for (int j = 0; j < NX; ++j) Y[i][j] = sn.L[i][j];
+    Y[i][NX] = sn.m[i] - mp[i];
   }
-  R Z[NX][WC];
-  SS_UNROLL
-  for (int i = 0; i < NX; ++i) {
-    SS_UNROLL
-    for (int j = 0; j < NX; ++j) {
-      R a = R(0), b = R(0);
-      SS_UNROLL
-      for (int k = j; k < NX; ++k) {
-        a += M[i][k] * sn.L[k][j];
-        b += l.F[i][k] * se.D[k][j];
-      }
-      Z[i][j] = a;
-      Z[i][NX + j] = b;
-    }
-    R e = sn.m[i] - l.bq[i];
-    SS_UNROLL
-    for (int k = 0; k < NX; ++k) e -= l.F[i][k] * mp[k];
-    Z[i][2 * NX] = e;
-  }
-  solve_lower<R, NX, WC>(l.cQ, Z);
+  solve_lower<R, NX, NX + 1>(X, Y);
+  R Ap[NX][NX];
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
     for (int j = 0; j < NX; ++j) {
       R q = (i == j) ? R(-1) : R(0);
       SS_UNROLL
-      for (int k = 0; k < WC; ++k) q += Z[i][k] * Z[j][k];
-      o.A[i][j] = q;
-    }
-  }
-  R EL[NX][NX];  // E Ls_t
-  SS_UNROLL
-  for (int i = 0; i < NX; ++i) {
-    SS_UNROLL
-    for (int j = 0; j < NX; ++j) {
-      R q = R(0);
-      SS_UNROLL
-      for (int k = j; k < NX; ++k) q += se.E[i][k] * sn.L[k][j];
-      EL[i][j] = q;
+      for (int k = 0; k < NX; ++k) q += Y[i][k] * Y[j][k];
+      Ap[i][j] = q;
+      o.N[i][j] = q + Y[i][NX] * Y[j][NX];
+      o.Lp[i][j] = (j <= i) ? X[i][j] : R(0);
     }
   }
   SS_UNROLL
   for (int i = 0; i < NX; ++i) {
     SS_UNROLL
     for (int j = 0; j < NX; ++j) {
-      R q = Z[i][2 * NX] * mp[j];
+      R q = Y[i][NX] * msp[j];
       SS_UNROLL
-      for (int k = 0; k < NX; ++k) q += Z[i][k] * EL[j][k] - Z[i][NX + k] * se.D[j][k];
+      for (int k = 0; k < NX; ++k) q += Ap[i][k] * X[NX + j][k];
       o.Fbar[i][j] = q;
     }
   }
-  solve_lower_T<R, NX, NX>(l.cQ, o.Fbar);
+  solve_lower_T<R, NX, NX>(X, o.Fbar);
   R zb[NX][1];
   SS_UNROLL
-  for (int i = 0; i < NX; ++i) zb[i][0] = Z[i][2 * NX];
-  solve_lower_T<R, NX, 1>(l.cQ, zb);
+  for (int i = 0; i < NX; ++i) zb[i][0] = Y[i][NX];
+  solve_lower_T<R, NX, 1>(X, zb);
   SS_UNROLL
   for (int i = 0; i < NX; ++i) o.bbar[i] = zb[i][0];
 }
@@ -208,6 +191,8 @@ SS_DEV void noise_factor_adjoint(const R (&c)[D][D], const R (&A)[D][D], const R
 
 template <typename R>
 struct AdjArgs {
+  const R* fm;      // filtered trajectory (caller layout)
+  const R* fL;
   const R* sm;      // smoothed trajectory (caller layout)
   const R* sL;
   const R* nom_m;   // the nominal (null: zero means, identity factors)
@@ -264,13 +249,13 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_chunk_kernel(ScanArgs<R> a,
     R y[NY];
     State<R, NX> sn;
     load_step<R, NX, NY>(a, b, i, base, t, l, y, sn);
-    SElem<R, NX> se;
-    load_se<R, NX>(a.selem + (base + t) * Rec<R, NX, NY>::SE_P, se);
-    R mp[NX];
-    load_prev_mean<R, NX>(b, base + i + t, mp);
+    State<R, NX> f;
+    load_traj<R, NX>(b.fm, b.fL, base + i + t, f);
+    R msp[NX];
+    load_prev_mean<R, NX>(b, base + i + t, msp);
     {
       AdjTrans<R, NX, NY> tr;
-      adjoint_transition<R, NX, NY>(l, se, mp, sn, tr);
+      adjoint_transition<R, NX, NY>(l, f, msp, sn, tr);
       SS_UNROLL
       for (int r = 0; r < NX; ++r) {
         SS_UNROLL
@@ -278,7 +263,7 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_chunk_kernel(ScanArgs<R> a,
         acc(K::B + r) += (double)tr.bbar[r];
       }
       R G[NX][NX];
-      noise_factor_adjoint<R, NX>(l.cQ, tr.A, Lq, G);
+      noise_factor_adjoint<R, NX>(tr.Lp, tr.N, Lq, G);
       SS_UNROLL
       for (int r = 0; r < NX; ++r) {
         SS_UNROLL
@@ -328,21 +313,25 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_param_kernel(ScanArgs<R> a,
     R y[NY];
     State<R, NX> sn;
     load_step<R, NX, NY>(a, b, i, base, t, l, y, sn);
-    R Fbar[DOUT][NX], bbar[DOUT], A[DOUT][DOUT], c[DOUT][DOUT];
+    // the step's adjoints and its noise-covariance adjoint as W^-T Cq W^-1 / 2 (W the
+    // whitening factor: the predicted factor for the transition, the observation's
+    // noise factor itself; Cq the core matrix), with the factor c of the linearised noise
+    R Fbar[DOUT][NX], bbar[DOUT], Cq[DOUT][DOUT], W[DOUT][DOUT], c[DOUT][DOUT];
     if constexpr (WHICH == 0) {
-      SElem<R, NX> se;
-      load_se<R, NX>(a.selem + (base + t) * Rec<R, NX, NY>::SE_P, se);
-      R mp[NX];
-      load_prev_mean<R, NX>(b, base + i + t, mp);
+      State<R, NX> f;
+      load_traj<R, NX>(b.fm, b.fL, base + i + t, f);
+      R msp[NX];
+      load_prev_mean<R, NX>(b, base + i + t, msp);
       AdjTrans<R, NX, NY> tr;
-      adjoint_transition<R, NX, NY>(l, se, mp, sn, tr);
+      adjoint_transition<R, NX, NY>(l, f, msp, sn, tr);
       SS_UNROLL
       for (int r = 0; r < NX; ++r) {
         bbar[r] = tr.bbar[r];
         SS_UNROLL
         for (int q = 0; q < NX; ++q) {
           Fbar[r][q] = tr.Fbar[r][q];
-          A[r][q] = tr.A[r][q];
+          Cq[r][q] = tr.N[r][q];
+          W[r][q] = tr.Lp[r][q];
           c[r][q] = l.cQ[r][q];
         }
       }
@@ -356,11 +345,20 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_param_kernel(ScanArgs<R> a,
         for (int q = 0; q < NX; ++q) Fbar[r][q] = ob.Hbar[r][q];
         SS_UNROLL
         for (int q = 0; q < NY; ++q) {
-          A[r][q] = ob.A[r][q];
+          Cq[r][q] = ob.A[r][q];
+          W[r][q] = l.cR[r][q];
           c[r][q] = l.cR[r][q];
         }
       }
     }
+    // tr(Qbar d(c c^T)) = tr(Cq U V^T), U = W^-1 dc, V = W^-1 c
+    R V[DOUT][DOUT];
+    SS_UNROLL
+    for (int r = 0; r < DOUT; ++r) {
+      SS_UNROLL
+      for (int q = 0; q < DOUT; ++q) V[r][q] = c[r][q];
+    }
+    solve_lower<R, DOUT, DOUT>(W, V);
     // the nominal at t - 1 (transition) or t (observation), the model noise
     R m[NX], C[NX][NX], qm[DOUT], qL[DOUT][DOUT];
     load_nominal<R, NX>(b.nom_m, b.nom_L, base + i + t + WHICH, m, C);
@@ -392,14 +390,13 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_param_kernel(ScanArgs<R> a,
       f.init(ma);
       D dF[DOUT][NX], dc[DOUT][DOUT], db[DOUT];
       linearize<D, NX, DOUT, Fn<D, NX, DOUT>, METHOD>(f, dm, dC, dqm, dqL, la.rule, la.slr_form, dF, dc, db);
-      // c^-1 dc
-      R X[DOUT][DOUT];
+      R U[DOUT][DOUT];
       SS_UNROLL
       for (int r = 0; r < DOUT; ++r) {
         SS_UNROLL
-        for (int q = 0; q < DOUT; ++q) X[r][q] = dc[r][q].d[0];
+        for (int q = 0; q < DOUT; ++q) U[r][q] = dc[r][q].d[0];
       }
-      solve_lower<R, DOUT, DOUT>(c, X);
+      solve_lower<R, DOUT, DOUT>(W, U);
       R s = R(0);
       SS_UNROLL
       for (int r = 0; r < DOUT; ++r) {
@@ -407,7 +404,12 @@ __global__ void __launch_bounds__(ADJ_BLOCK) adjoint_param_kernel(ScanArgs<R> a,
         SS_UNROLL
         for (int q = 0; q < NX; ++q) s += Fbar[r][q] * dF[r][q].d[0];
         SS_UNROLL
-        for (int q = 0; q < DOUT; ++q) s += A[r][q] * X[q][r];
+        for (int q = 0; q < DOUT; ++q) {
+          R cu = R(0);
+          SS_UNROLL
+          for (int k = 0; k < DOUT; ++k) cu += Cq[r][k] * U[k][q];
+          s += cu * V[r][q];
+        }
       }
       g[d] += (double)s;
     }
@@ -503,15 +505,20 @@ inline int param_mask(int kind) {
 
 struct AdjLayout {
   Layout inner;
-  size_t part, bytes;
+  size_t part, fm, fL, bytes;
 };
 
+// The scan's workspace, then the partial sums and the filtered trajectory (the
+// smoothed one goes to the scan's nominal buffers, which this call does not use).
 template <typename R, int NX, int NY>
 inline int make_adj_layout(const ss_problem& p, AdjLayout& y) {
   int rc = make_layout<R, NX, NY>(p, y.inner);
   if (rc) return rc;
+  const size_t S = (size_t)(p.total_steps + p.batch);
   y.part = y.inner.bytes;
-  y.bytes = y.part + align_up(sizeof(double) * (size_t)y.inner.items[1] * AdjK<NX, NY>::K);
+  y.fm = y.part + align_up(sizeof(double) * (size_t)y.inner.items[1] * AdjK<NX, NY>::K);
+  y.fL = y.fm + align_up(sizeof(R) * S * NX);
+  y.bytes = y.fL + align_up(sizeof(R) * S * NX * NX);
   return SS_OK;
 }
 
@@ -585,9 +592,11 @@ int run_adjoint(const Call& c) {
   R* sm = rn.template at<R>(rn.y.nomA_m);
   R* sL = rn.template at<R>(rn.y.nomA_L);
   double* part = rn.template at<double>(y.part);
-  // filter with the smoothing elements and the log-likelihood partial sums
-  rn.sa.filt_m = nullptr;
-  rn.sa.filt_L = nullptr;
+  // filter with the smoothing elements, the filtered trajectory and the log-likelihood partial sums
+  R* fm = rn.template at<R>(y.fm);
+  R* fL = rn.template at<R>(y.fL);
+  rn.sa.filt_m = fm;
+  rn.sa.filt_L = fL;
   rn.sa.ll_chunk = rn.template at<double>(rn.y.ll);
   if ((rc = rn.filter_pass(true))) return rc;
   if (c.out_ell != nullptr)
@@ -602,7 +611,11 @@ int run_adjoint(const Call& c) {
   rn.sa.mse = nullptr;
   rn.sa.flags = nullptr;
   if ((rc = rn.smoother_scan_and_walk())) return rc;
+  rn.sa.filt_m = nullptr;
+  rn.sa.filt_L = nullptr;
   AdjArgs<R> b;
+  b.fm = fm;
+  b.fL = fL;
   b.sm = sm;
   b.sL = sL;
   b.nom_m = nm;

@@ -126,3 +126,28 @@ def test_bearings_parameter_gradient_matches_finite_differences(method):
     fd = np.array([(ell_of(theta + h * e) - ell_of(theta - h * e)) / (2 * h) for e in np.eye(4)])
     assert np.isclose(ell, ell_of(theta))
     np.testing.assert_allclose(g, fd, rtol=2e-6, atol=1e-6 * np.abs(fd).max())
+
+
+@pytest.mark.parametrize("method", ["extended", "cubature"])
+def test_predicted_moment_form_equals_residual_form(method):
+    """The GPU kernel's transition contraction (predicted moments, no state differences) equals
+    the residual form of filter_adjoint: dl/dF, dl/db and dl/dQ = cQ^-T A_q cQ^-1 / 2."""
+    from sqrt_parallel_smoothers_gb300 import data
+    T = 30
+    w = data.bearings_workload(T, seed=4)
+    ys = w["ys"].astype(float)
+    Q1, _ = OM.bearings_noise(1.0, 5.0, 0.05, 0.01)
+    m0 = np.array([0.1, 0.2, 1.0, 0.0, 1.0])
+    x0 = O.MVNSqrt(m0, np.eye(5))
+    tm, om = _bearings_models(np.array([-1.5, 0.5, np.log(0.1), np.log(0.05)]), Q1)
+    lin = getattr(O.linearization, method)
+    nom = O.MVNSqrt(np.repeat(m0[None], T + 1, 0), np.repeat(0.3 * np.eye(5)[None], T + 1, 0))
+    _, adj = adjoint.filter_adjoint(ys, x0, tm, om, lin, nom)
+    F, cQ, b = adj["lin"][:3]
+    filt = O.parallel.filtering(ys, x0, tm, om, lin, nom)
+    sm = O.parallel.smoothing(tm, filt, lin, nom)
+    Fbar, bbar, Qbar = adjoint.transition_adjoint_predicted_form(F, cQ, b, np.asarray(filt[0]), np.asarray(filt[1]),
+                                                                 np.asarray(sm[0]), np.asarray(sm[1]))
+    Qbar_res = 0.5 * adjoint._unwhiten_T(cQ, np.swapaxes(adjoint._unwhiten_T(cQ, adj["A_q"]), -1, -2))
+    for got, ref in ((Fbar, adj["F"]), (bbar, adj["b"]), (Qbar, Qbar_res)):
+        np.testing.assert_allclose(got, ref, rtol=1e-7, atol=1e-9 * np.abs(ref).max())
