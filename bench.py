@@ -789,6 +789,11 @@ def gpu_arm(args):
         if rank == 0:
             print(json.dumps(large_state_section(torch, S, flush, T=args.large_T, compare=False)), flush=True)
         return 0
+    if args.only_adjoint:
+        flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+        if rank == 0:
+            print(json.dumps(adjoint_section(torch, S, flush)), flush=True)
+        return 0
     lengths, batch = rank_batch(S, args.batch, rank)
     offsets = batch["offsets"]
     tuning = None
@@ -986,6 +991,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="skip the T sweep and the large-state workload")
     ap.add_argument("--only-large", action="store_true", help="run the large-state workload only")
     ap.add_argument("--large-T", type=int, default=131_072, help="sequence length of the large-state workload")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="run the gradient workloads only (reverse and tangent passes, p = 4 and p = 32)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
