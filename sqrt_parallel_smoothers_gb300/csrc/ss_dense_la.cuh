@@ -168,6 +168,9 @@ struct Tria {
   template <int J0>
   static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
     constexpr int JB = (J0 + 8 < CP) ? J0 + 8 : CP;   // end of the pivot block's columns
+    // rows r < J0 are final: from pivot 32 on, a lane's first slot (rows 0..31)
+    // takes no more reflector work (a warp-wide saving, not a per-lane mask)
+    constexpr int S0 = (J0 >= 32) ? 1 : 0;
     const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
     for (int p = J0; p < pend; ++p) {
       R* v = vb + (p & 1) * VS;
@@ -210,7 +213,7 @@ struct Tria {
       }
       R d[NS][4];
       SS_UNROLL
-      for (int s = 0; s < NS; ++s) {
+      for (int s = S0; s < NS; ++s) {
         SS_UNROLL
         for (int k = 0; k < 4; ++k) d[s][k] = R(0);
       }
@@ -220,7 +223,7 @@ struct Tria {
         SS_UNROLL
         for (int u = 0; u < W; ++u) {
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) {
+          for (int s = S0; s < NS; ++s) {
             R vj = x.v[u];
             if (j + u < JB) vj += cb[j + u - J0];
             d[s][(j + u) & 3] += row[s][j + u] * vj;
@@ -229,7 +232,7 @@ struct Tria {
       }
       R f[NS];
       SS_UNROLL
-      for (int s = 0; s < NS; ++s) {
+      for (int s = S0; s < NS; ++s) {
         const int r = lane + 32 * s;
         const R dd = (d[s][0] + d[s][1]) + (d[s][2] + d[s][3]);
         f[s] = (r >= p && r < ROWS) ? tau * dd : R(0);
@@ -242,7 +245,7 @@ struct Tria {
           R vj = x.v[u];
           if (j + u < JB) vj += cb[j + u - J0];
           SS_UNROLL
-          for (int s = 0; s < NS; ++s) row[s][j + u] -= f[s] * vj;
+          for (int s = S0; s < NS; ++s) row[s][j + u] -= f[s] * vj;
         }
       }
     }
