@@ -715,10 +715,21 @@ def large_state_section(torch, S, flush, chunk=32, T=131_072, compare=True):
                                       graph=True)
         ms_ps, _ = time_plan(torch, plan, 2, 1, flush)
         del plan
+        torch.cuda.empty_cache()
+        pplan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None,
+                                       criterion=S.FixedIterations(9), offsets=offsets, chunk=chunk, group=8,
+                                       graph=True, profile=True)
+        pplan.run()
+        torch.cuda.synchronize()
+        prof_ps = _lib.profile_read()
+        del pplan
+        _lib.profile_reset()
     finally:
         S.set_large_state_options(per_sequence_covariance=False)
     torch.cuda.empty_cache()
     per_seq_ms = float(np.median(ms_ps))
+    tot_ps = sum(v[1] for v in prof_ps.values()) or 1.0
+    kern_ps = {k: {"launches": v[0], "total_ms": v[1], "share": v[1] / tot_ps} for k, v in prof_ps.items()}
     pplan = S.IteratedSmootherPlan(y32, x0, tm, om, S.linearization.cubature, None, criterion=S.FixedIterations(9),
                                    offsets=offsets, chunk=chunk, group=8, graph=True, profile=True)
     pplan.run()
@@ -746,7 +757,8 @@ def large_state_section(torch, S, flush, chunk=32, T=131_072, compare=True):
            "mode": "shared covariance (one prior, equal lengths): factors once per time step, means per sequence",
            "ms_per_step": step_ms, "timesteps_per_s": B * T / (step_ms * 1e-3), "gpu_launches": launches,
            "per_sequence_covariance": {"ms_per_step": per_seq_ms, "timesteps_per_s": B * T / (per_seq_ms * 1e-3),
-                                       "mode": "every sequence's factors computed separately (the general batch)"},
+                                       "mode": "every sequence's factors computed separately (the general batch)",
+                                       "kernels": kern_ps},
            "kernels": kern, "roofline": roof}
     if not compare:
         return out

@@ -213,10 +213,17 @@ struct DRunner {
       SS_LAUNCH("filter_down", st, down_kernel<R, NX, NY><<<(unsigned)y.items[l + 1], 32, sm_ap, st>>>(a, l));
     }
     a.s.emit_smoother = emit_smoother ? 1 : 0;
-    constexpr int WW = walk_warps<R, NX, NY>();
-    const size_t sm_w = sizeof(R) * walk_elems<R, NX, NY>();
-    set_smem(walk_kernel<R, NX, NY>, sm_w);
-    SS_LAUNCH("filter_walk", st, walk_kernel<R, NX, NY><<<grid_for(y.items[1], WW), 32 * WW, sm_w, st>>>(a));
+    if constexpr (std::is_same<R, float>::value) {
+      const size_t sm_r = sizeof(R) * walk_r_elems<R, NX, NY>();
+      set_smem(walk_r_kernel<R, NX, NY>, sm_r);
+      SS_LAUNCH("filter_walk", st,
+                walk_r_kernel<R, NX, NY><<<grid_for(y.items[1], WALK_R_WARPS), 32 * WALK_R_WARPS, sm_r, st>>>(a));
+    } else {
+      constexpr int WW = walk_warps<R, NX, NY>();
+      const size_t sm_w = sizeof(R) * walk_elems<R, NX, NY>();
+      set_smem(walk_kernel<R, NX, NY>, sm_w);
+      SS_LAUNCH("filter_walk", st, walk_kernel<R, NX, NY><<<grid_for(y.items[1], WW), 32 * WW, sm_w, st>>>(a));
+    }
     return SS_OK;
   }
 

@@ -582,6 +582,159 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
   }
 }
 
+// ----------------------------------------------------------------------------- per-sequence walk, register rows
+
+// The per-sequence Kalman walk (walk_kernel's results, up to rounding) with Phi
+// and Psi built and triangularised in registers as walk_b_kernel does: only the
+// factor, Psi's blocks and the vectors go through shared memory, about 9 KB per
+// warp against walk_kernel's 23 KB (whose Phi region alone is 17 KB), so the
+// SM holds more warps.  FP32 (the rows of an FP64 Phi would not fit the
+// register file).
+template <typename R, int NX, int NY>
+__host__ __device__ constexpr int walk_r_warp_elems() {
+  typedef DS<R, NX, NY> S;
+  return S::MN + (NY + NX) * S::LDY + 2 * S::VN + S::VY +
+         2 * (Pad<R, (2 * NX > NX + NY ? 2 * NX : NX + NY)>::n + Vec<R>::n);
+}
+constexpr int WALK_R_WARPS = 2;
+#ifndef WALK_R_MINB
+#define WALK_R_MINB 1
+#endif
+template <typename R, int NX, int NY>
+__host__ __device__ constexpr int walk_r_elems() {
+  return mc_elems<R, NX, NY>() + WALK_R_WARPS * walk_r_warp_elems<R, NX, NY>();
+}
+
+template <typename R, int NX, int NY>
+__global__ void __launch_bounds__(32 * WALK_R_WARPS, WALK_R_MINB) walk_r_kernel(DenseArgs<R> a) {
+  typedef DS<R, NX, NY> S;
+  constexpr int W = S::W;
+  constexpr int NSF = (2 * NX + 31) / 32, CPF = Pad<R, 2 * NX>::n;
+  constexpr int NSP = (NX + NY + 31) / 32, CPP = Pad<R, NX + NY>::n;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* p = reinterpret_cast<R*>(smem_raw);
+  const int warp = threadIdx.x >> 5, l = lane_id();
+  MC<R> c = carve_mc<R, NX, NY>(p);
+  p += warp * walk_r_warp_elems<R, NX, NY>();
+  zero(p, walk_r_warp_elems<R, NX, NY>());
+  if (warp == 0) load_mc<R, NX, NY>(c, a);
+  __syncthreads();
+  R* L = p; p += S::MN;
+  R* P11 = p; p += NY * S::LDY;
+  R* P21 = p; p += NX * S::LDY;
+  R* m = p; p += S::VN;
+  R* mp = p; p += S::VN;
+  R* rv = p; p += S::VY;
+  R* vb = p;
+  const ScanArgs<R>& sa = a.s;
+  const int64_t j = (int64_t)blockIdx.x * WALK_R_WARPS + warp;
+  if (j >= sa.g.lvl[1][sa.g.B]) return;
+  int64_t i, t0, t1;
+  chunk_of(sa.g, j, i, t0, t1);
+  if (seq_inactive(sa.active, i)) return;
+  const int64_t base = sa.g.off[i];
+  load_st<R, NX, NY>(L, m, sa.fst[1] + j * S::ST);
+  double ll = 0.0;
+  for (int64_t t = t0; t < t1; ++t) {
+    R* rec = sa.selem + (base + t) * S::SE;
+    {
+      // Phi = tria([[F L, cQ], [L, 0]]): Phi11 -> L (the predicted factor N1), and
+      // per row of Phi21 E = Phi21 Phi11^{-1}, D = Phi22 and g = m - E mp into the record
+      R row[NSF][CPF];
+      phi_rows<R, NX, NY>(c, L, row);
+      const R mpl = rowdot<R, NX, NX, false, S::LDN>(c.F, m, l) + (l < NX ? c.bq[l] : R(0));
+      __syncwarp();
+      Tria<R, 2 * NX, 2 * NX, CPF>::run_regs(row, vb);
+      if (l < NX) mp[l] = mpl;
+      SS_UNROLL
+      for (int s = 0; s < NSF; ++s) {
+        const int r = l + 32 * s;
+        if (r < NX) store_part<R, NX, S::LDN, 0>(L, r, row[s]);
+      }
+      __syncwarp();
+      SS_UNROLL
+      for (int s = 0; s < NSF; ++s) {
+        const int r = l + 32 * s;
+        if (r >= NX && r < 2 * NX && sa.emit_smoother) {
+          SS_UNROLL
+          for (int k = NX - 1; k >= 0; --k) {
+            row[s][k] = row[s][k] * ss_rcp(L[k * S::LDN + k]);
+            SS_UNROLL
+            for (int jj = 0; jj < k; jj += W) {
+              const Vec<R> lv = ld16(L + k * S::LDN + jj);
+              SS_UNROLL
+              for (int u = 0; u < W; ++u)
+                if (jj + u < k) row[s][jj + u] -= row[s][k] * lv.v[u];
+            }
+          }
+          R g = m[r - NX];
+          SS_UNROLL
+          for (int k = 0; k < NX; ++k) g -= row[s][k] * mp[k];
+          R* de = rec + (r - NX) * NX;
+          R* dd = rec + NX * NX + (r - NX) * NX;
+          SS_UNROLL
+          for (int jj = 0; jj < NX; jj += W) {
+            Vec<R> oe, od;
+            SS_UNROLL
+            for (int u = 0; u < W; ++u) {
+              oe.v[u] = row[s][jj + u];
+              od.v[u] = row[s][NX + jj + u];
+            }
+            st16(de + jj, oe);
+            st16(dd + jj, od);
+          }
+          rec[2 * NX * NX + r - NX] = g;
+        }
+      }
+      __syncwarp();
+    }
+    {
+      // update: Psi = tria([[H N1, cR], [N1, 0]]): Psi11 -> P11, Psi21 -> P21, Psi22 -> L
+      R row[NSP][CPP];
+      psi_rows<R, NX, NY>(c, L, row);
+      __syncwarp();
+      Tria<R, NX + NY, NX + NY, CPP>::run_regs(row, vb);
+      SS_UNROLL
+      for (int s = 0; s < NSP; ++s) {
+        const int r = l + 32 * s;
+        if (r < NY) {
+          store_part<R, NY, S::LDY, 0>(P11, r, row[s]);
+        } else if (r < NY + NX) {
+          store_part<R, NY, S::LDY, 0>(P21, r - NY, row[s]);
+          store_part<R, NX, S::LDN, NY>(L, r - NY, row[s]);
+        }
+      }
+      __syncwarp();
+    }
+    const R res = (l < NY ? sa.ys[(base + t) * NY + l] - c.c[l] : R(0)) - rowdot<R, NY, NX, false, S::LDN>(c.H, mp, l);
+    if (l < NY) rv[l] = res;
+    __syncwarp();
+    R z[NY];
+    R q = R(0), ld = R(0);
+    SS_UNROLL
+    for (int k = 0; k < NY; ++k) {
+      R t2 = rv[k];
+      SS_UNROLL
+      for (int jj = 0; jj < k; ++jj) t2 -= P11[k * S::LDY + jj] * z[jj];
+      const R dk = P11[k * S::LDY + k];
+      z[k] = t2 / dk;
+      q += z[k] * z[k];
+      ld += ss_log(ss_abs(dk));
+    }
+    ll += -0.5 * ((double)q + 2.0 * (double)ld);
+    const int il = l < NX ? l : NX - 1;
+    R mn = mp[il];
+    SS_UNROLL
+    for (int k = 0; k < NY; ++k) mn += P21[il * S::LDY + k] * z[k];
+    __syncwarp();
+    if (l < NX) m[l] = mn;
+    __syncwarp();
+    if (sa.filt_m != nullptr) store_traj<R, NX, NY>(sa.filt_m, sa.filt_L, base + i + t + 1, L, m);
+  }
+  if (sa.ll_chunk != nullptr && l == 0) sa.ll_chunk[j] = ll;
+  if (t1 == sa.g.off[i + 1] - base) store_st<R, NX, NY>(sa.fT + i * S::ST, L, m);
+}
+
 // ----------------------------------------------------------------------------- smoother
 
 template <typename R, int NX, int NY>
