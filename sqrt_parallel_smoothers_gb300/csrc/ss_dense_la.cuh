@@ -156,7 +156,11 @@ SS_DEV void parlett(float x0, float sig, float& v0, float& tau) {
 // is cleared once at the end.  Pivots are processed in blocks of eight so that
 // every register index is compile-time.  vb holds two buffers of
 // Pad<COLS>::n + W elements (16-byte aligned): tria_scratch().
-template <typename R, int ROWS, int COLS, int LD>
+// ROLL: the pivot loop of a block needs no compile-time pivot index; kept
+// rolled, the code of the large triangularisations shrinks (measured: the
+// per-sequence walk and the scan levels 10 % faster, fewer instruction-cache
+// stalls), while the shared-covariance walk measured 7 % faster unrolled.
+template <typename R, int ROWS, int COLS, int LD, bool ROLL = true>
 struct Tria {
   static constexpr int W = Vec<R>::n;
   static constexpr int CP = Pad<R, COLS>::n;
@@ -167,12 +171,22 @@ struct Tria {
 
   template <int J0>
   static SS_DEV void block(R (&row)[NS][CP], R* vb, int lane) {
-    constexpr int JB = (J0 + 8 < CP) ? J0 + 8 : CP;   // end of the pivot block's columns
     // rows r < J0 are final: from pivot 32 on, a lane's first slot (rows 0..31)
     // takes no more reflector work (a warp-wide saving, not a per-lane mask)
     constexpr int S0 = (J0 >= 32) ? 1 : 0;
     const int pend = (J0 + 8 < ROWS) ? J0 + 8 : ROWS;
-    for (int p = J0; p < pend; ++p) {
+    if constexpr (ROLL) {
+#pragma unroll 1
+      for (int p = J0; p < pend; ++p) pivot<J0, S0>(p, row, vb, lane);
+    } else {
+      for (int p = J0; p < pend; ++p) pivot<J0, S0>(p, row, vb, lane);
+    }
+  }
+
+  template <int J0, int S0>
+  static SS_DEV void pivot(int p, R (&row)[NS][CP], R* vb, int lane) {
+    constexpr int JB = (J0 + 8 < CP) ? J0 + 8 : CP;   // end of the pivot block's columns
+    {
       R* v = vb + (p & 1) * VS;
       if (lane == (p & 31)) {
         const int ps = p >> 5;

@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
       R row[NSF][CPF];
       phi_rows<R, NX, NY>(c, L, row);
       __syncwarp();
-      Tria<R, 2 * NX, 2 * NX, CPF>::run_regs(row, vb);
+      Tria<R, 2 * NX, 2 * NX, CPF, false>::run_regs(row, vb);
       SS_UNROLL
       for (int s = 0; s < NSF; ++s) {
         const int r = l + 32 * s;
@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(32 * walk_b_warps<R, NX, NY>())
       R row[NSP][CPP];
       psi_rows<R, NX, NY>(c, L, row);
       __syncwarp();
-      Tria<R, NX + NY, NX + NY, CPP>::run_regs(row, vb);
+      Tria<R, NX + NY, NX + NY, CPP, false>::run_regs(row, vb);
       SS_UNROLL
       for (int s = 0; s < NSP; ++s) {
         const int r = l + 32 * s;
