@@ -245,6 +245,41 @@ struct PatFull {
   __host__ __device__ static constexpr bool nz(int, int) { return true; }
 };
 
+// Reflector I of tria_sp applied to the rows it touches: M[r] += c u with
+// u = (v0, M[I][I+1:]) and c = k (M[r] . u).
+template <typename R, int ROWS, int COLS, int I, unsigned long long SUP, unsigned long long TOUCH>
+SS_DEV void tria_sp_apply(R (&M)[ROWS][COLS], const R& v0, const R& k) {
+  constexpr int i = I;
+  SS_UNROLL
+  for (int r = i + 1; r < ROWS; ++r) {
+    if ((TOUCH >> r) & 1) {
+      R d0 = M[r][i] * v0, d1 = R(0);
+      SS_UNROLL
+      for (int j = i + 1; j < COLS; ++j) {
+        if ((SUP >> j) & 1) {
+          if ((j - i) & 1) d1 += M[r][j] * M[i][j];
+          else d0 += M[r][j] * M[i][j];
+        }
+      }
+      const R c = (d0 + d1) * k;
+      M[r][i] += c * v0;
+      SS_UNROLL
+      for (int j = i + 1; j < COLS; ++j)
+        if ((SUP >> j) & 1) M[r][j] += c * M[i][j];
+    }
+  }
+}
+
+// A row whose part right of the diagonal is already zero (sigma == 0) needs no
+// reflector.  With SS_TRIA_SELECT that case is taken by selects (v0 = k = 0
+// makes the update a no-op, beta = x0) instead of a branch around the
+// reflector, so the code of a triangularisation is one basic block and the
+// scheduler can overlap each reflector's row updates with the next one's norm
+// (the range guard's rare rescaling keeps its branch).
+#ifndef SS_TRIA_SELECT
+#define SS_TRIA_SELECT 1
+#endif
+
 template <typename R, int ROWS, int COLS, class PAT, int I, bool GUARD>
 SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
   if constexpr (I < ROWS) {
@@ -264,12 +299,13 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
       }
       R sigma = sig0 + sig1;
       R x0 = M[i][i];
-      if (sigma != R(0)) {
+      const bool live = sigma != R(0);
+      if (SS_TRIA_SELECT || live) {
         // H = I + u u^T / (beta v0), u = (v0, M[i][i+1:]), v0 = x0 - beta:
         // one reciprocal per reflector, no scaled copy of the row (except in
         // the FP32 range guard, which scales the row in place).
-        R v0, k, unscale = R(1);
-        if (GUARD && reflector_out_of_range(x0, sigma)) {
+        R v0, k, b, unscale = R(1);
+        if (GUARD && live && reflector_out_of_range(x0, sigma)) {
           R amax = ss_abs(x0);
           SS_UNROLL
           for (int j = i + 1; j < COLS; ++j)
@@ -286,26 +322,11 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
             }
           }
         }
-        reflector(x0, sigma, beta, v0, k);
-        beta *= unscale;
-        SS_UNROLL
-        for (int r = i + 1; r < ROWS; ++r) {
-          if ((TOUCH >> r) & 1) {
-            R d0 = M[r][i] * v0, d1 = R(0);
-            SS_UNROLL
-            for (int j = i + 1; j < COLS; ++j) {
-              if ((SUP >> j) & 1) {
-                if ((j - i) & 1) d1 += M[r][j] * M[i][j];
-                else d0 += M[r][j] * M[i][j];
-              }
-            }
-            const R c = (d0 + d1) * k;
-            M[r][i] += c * v0;
-            SS_UNROLL
-            for (int j = i + 1; j < COLS; ++j)
-              if ((SUP >> j) & 1) M[r][j] += c * M[i][j];
-          }
-        }
+        reflector(x0, sigma, b, v0, k);
+        beta = live ? b * unscale : beta;
+        v0 = live ? v0 : R(0);
+        k = live ? k : R(0);
+        tria_sp_apply<R, ROWS, COLS, I, SUP, TOUCH>(M, v0, k);
       }
     }
     SS_UNROLL
