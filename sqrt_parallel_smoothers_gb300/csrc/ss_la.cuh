@@ -89,6 +89,21 @@ SS_DEV float pow2_inverse_scale(float amax) {
 template <typename R>
 SS_DEV R pow2_inverse_scale(const R&) { return R(1); }
 
+// Whether row i still needs a reflector.  In FP32 a row whose whole sum of
+// squares x0^2 + sigma is below the smallest normal float is taken as already
+// reduced: the hardware reciprocal square root flushes such a denormal to zero
+// and would turn the reflector into inf * 0 = NaN, while the entries it would
+// rotate are below 1.1e-19, far under the rounding of any normal-range factor.
+// (The range-guarded triangularisations rescale such rows instead.)
+#ifndef SS_TINY_ROWS_REDUCED
+#define SS_TINY_ROWS_REDUCED 1
+#endif
+template <typename R>
+SS_DEV bool reflector_live(const R& x0, const R& sigma) { return sigma != R(0); }
+SS_DEV bool reflector_live(float x0, float sigma) {
+  return sigma != 0.0f && (!SS_TINY_ROWS_REDUCED || x0 * x0 + sigma >= 0x1p-126f);
+}
+
 // Programmatic dependent launch (sm_90 and later).  The per-pass kernels are
 // launched with programmatic stream serialisation, so a kernel's launch is
 // prepared while its predecessor on the stream drains.  Each such kernel calls
@@ -299,7 +314,7 @@ SS_DEV void tria_sp_step(R (&M)[ROWS][COLS]) {
       }
       R sigma = sig0 + sig1;
       R x0 = M[i][i];
-      const bool live = sigma != R(0);
+      const bool live = GUARD ? sigma != R(0) : reflector_live(x0, sigma);
       if (SS_TRIA_SELECT || live) {
         // H = I + u u^T / (beta v0), u = (v0, M[i][i+1:]), v0 = x0 - beta:
         // one reciprocal per reflector, no scaled copy of the row (except in

@@ -180,7 +180,7 @@ def test_standard_fp32_linear_close_to_fp64():
     assert_rel(sm.cov, ref_s.cov, 2e-4, "smoothed cov")
 
 
-def _robustness_run(lin, T, dtype, form):
+def _robustness_run(lin, T, dtype, form, slr_form=0):
     """The reference's FP32 robustness study (notebooks/robustness_100runs.py): 20 runs, 20
     iterated calls from the nominal (-1, -1, 6, 4, 2), prior (-4, -1, 2, 7, 3)."""
     d = np.load(os.path.join(os.path.dirname(__file__), "golden", "robustness_small.npz"))
@@ -196,7 +196,7 @@ def _robustness_run(lin, T, dtype, form):
         nom = S.MVNStandard(torch.tensor([-1.0, -1.0, 6.0, 4.0, 2.0], dtype=dtype).expand(runs, T + 1, 5),
                             torch.eye(5, dtype=dtype).expand(runs, T + 1, 5, 5))
     _, ell = S.iterated_smoothing(torch.as_tensor(d["ys"][:, :T], dtype=dtype), x0, gt, go, lin, nom,
-                                  criterion=lambda i, *_: i < 20, return_loglikelihood=True)
+                                  criterion=lambda i, *_: i < 20, return_loglikelihood=True, slr_form=slr_form)
     return np_(ell), d
 
 
@@ -233,3 +233,15 @@ def test_robustness_covariance_form_extended_gpu(T):
     rel = np.abs(ell - g) / np.abs(g)
     assert np.isfinite(ell).all()
     assert np.mean(rel < 1e-4) >= 0.8, rel
+
+
+@pytest.mark.parametrize("T", [20, 50, 100])
+def test_robustness_fp32_downdate_slr_stays_finite(T):
+    """The reference's own SLR arithmetic in FP32 (Cholesky downdate, slr_form=1) on its
+    robustness study: the reference's FP32 square-root cubature log-likelihoods are finite on
+    every run, and so are these.  The downdate's cancellation leaves factor rows whose sum of
+    squares is below the smallest normal float; such rows count as already reduced (the
+    hardware reciprocal square root would flush them to zero and return NaN)."""
+    ell, d = _robustness_run(S.linearization.cubature, T, torch.float32, "sqrt", slr_form=1)
+    assert np.isfinite(d["ell_cubature"][list(d["Ts"]).index(T)]).all()
+    assert np.isfinite(ell).all(), ell
