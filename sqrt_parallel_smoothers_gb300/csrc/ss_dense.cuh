@@ -744,7 +744,9 @@ __host__ __device__ constexpr int walk_elems() {
 
 // Kalman steps of one chunk from its entry state; emits the smoothing elements.
 // Phi and then Psi share one shared-memory region: Phi11 (the predicted factor)
-// moves to the state buffer, whose old content Phi has consumed.
+// moves to the state buffer, whose old content Phi has consumed.  The FP64
+// walk; FP32 runs walk_r_kernel (ss_dense_shared.cuh), which keeps Phi and Psi
+// in registers.
 template <typename R, int NX, int NY>
 __global__ void __launch_bounds__(32 * walk_warps<R, NX, NY>()) walk_kernel(DenseArgs<R> a) {
   typedef DS<R, NX, NY> S;
