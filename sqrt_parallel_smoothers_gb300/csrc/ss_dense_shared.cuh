@@ -597,8 +597,11 @@ __host__ __device__ constexpr int walk_r_warp_elems() {
          2 * (Pad<R, (2 * NX > NX + NY ? 2 * NX : NX + NY)>::n + Vec<R>::n);
 }
 constexpr int WALK_R_WARPS = 2;
-#ifndef WALK_R_MINB
-#define WALK_R_MINB 1
+// Minimum resident blocks requested from the register allocator: one (229-242
+// registers, 4 blocks = 8 warps per SM); a cap of 168 registers for five blocks
+// spilled 644 bytes per thread.
+#ifndef SS_DENSE_WALK_MINB
+#define SS_DENSE_WALK_MINB 1
 #endif
 template <typename R, int NX, int NY>
 __host__ __device__ constexpr int walk_r_elems() {
@@ -606,7 +609,7 @@ __host__ __device__ constexpr int walk_r_elems() {
 }
 
 template <typename R, int NX, int NY>
-__global__ void __launch_bounds__(32 * WALK_R_WARPS, WALK_R_MINB) walk_r_kernel(DenseArgs<R> a) {
+__global__ void __launch_bounds__(32 * WALK_R_WARPS, SS_DENSE_WALK_MINB) walk_r_kernel(DenseArgs<R> a) {
   typedef DS<R, NX, NY> S;
   constexpr int W = S::W;
   constexpr int NSF = (2 * NX + 31) / 32, CPF = Pad<R, 2 * NX>::n;
